@@ -1,0 +1,216 @@
+/*
+ * dfcsr_gb300.h - C ABI of the GB300 (sm_103a) CSR wake path.
+ *
+ * The wake path of pyDFCSR_2D (deposit -> smoothing/derivatives -> history
+ * -> retarded-geometry CSR integral) as plain `extern "C"` entry points over
+ * device pointers and sizes.  No torch, numpy or CUDA types appear here:
+ * every `stream` is a `cudaStream_t` passed as `void *`, every array is a
+ * device pointer unless the comment says host.
+ *
+ * The reference has no FFI layer: its boundary is the Python method surface
+ * of DF_tracker / CSR2D and the numba functions.  Each entry point below
+ * names the reference function it replaces (file:line within pyDFCSR_2D/).
+ *
+ * Every call returns a dfcsr_status; on failure dfcsr_last_error() gives a
+ * message for the calling host thread.  Calls are asynchronous on `stream`
+ * unless stated otherwise; a call never synchronises the device.
+ */
+#ifndef DFCSR_GB300_H
+#define DFCSR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    DFCSR_OK = 0,
+    DFCSR_BAD_ARG = 1,          /* invalid size, null pointer, bad parameter */
+    DFCSR_OOM = 2,              /* workspace too small / allocation refused   */
+    DFCSR_TIMEOUT = 3,          /* a bounded device wait gave up              */
+    DFCSR_KERNEL_ERROR = 4,     /* a kernel reported an error status word     */
+    DFCSR_CUDA_ERROR = 5,       /* CUDA runtime error (launch, copy)          */
+    DFCSR_ADMISSION_REFUSED = 6 /* request does not fit the HBM budget        */
+} dfcsr_status;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int dfcsr_version(void);
+/* Message of the last failing call on this host thread ("" if none). */
+const char *dfcsr_last_error(void);
+/* Short name of a status code. */
+const char *dfcsr_status_name(int status);
+/* sizeof of the ABI structs: 0 dfcsr_df_params, 1 dfcsr_wake_job (for
+ * bindings that lay the structs out themselves); 0 for other values. */
+size_t dfcsr_abi_sizeof(int which);
+
+/* ------------------------------------------------------------------------
+ * Beam moments.  Replaces the numpy statistics used by DF_tracker.get_DF
+ * (deposit.py:147-159: std/mean of x and z, slice std of x where
+ * |z| < 0.1 sigma_z) and by Beam (beams.py:137-215: mean/std, polyfit
+ * slope of x on z, std/mean of the chirp-removed x_transform).
+ *
+ * out[16] (device, double): 0 n, 1 mean_x, 2 mean_z, 3 sigma_x, 4 sigma_z,
+ * 5 slope (dx/dz), 6 intercept, 7 n_slice, 8 sigma_x_slice, 9 mean_xt,
+ * 10 sigma_xt, 11 cov_xz, 12..15 reserved.  Deterministic (fixed reduction
+ * order).  Needs dfcsr_moments_workspace_bytes(n) bytes of device scratch.
+ */
+size_t dfcsr_moments_workspace_bytes(int64_t n);
+int dfcsr_beam_moments(const double *x, const double *z, int64_t n, double *out,
+                       void *workspace, size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Cloud-in-cell deposit.  Replaces histogram_cic_2d (deposit.py:43-87),
+ * called twice per step by get_DF (deposit.py:172-182) with w = 1 and
+ * w = px.  Both weight channels are deposited from one sort:
+ *   out0 = CIC(q1, q2, w0 or 1 if w0 == NULL)   [nb1][nb2] row-major
+ *   out1 = CIC(q1, q2, w1)                       (skipped if w1 == NULL)
+ * Bin spacing (end - start) / nbins, lower bin floor(cell), weights
+ * 1 - frac, bounds-checked corners - exactly the reference's rule.
+ * Deterministic: particles are sorted by lower cell (stable LSD radix sort)
+ * and each cell is summed by one warp in a fixed order.  No float atomics.
+ * Needs dfcsr_deposit_workspace_bytes(n, nb1, nb2) bytes of scratch.
+ */
+size_t dfcsr_deposit_workspace_bytes(int64_t n, int nb1, int nb2);
+int dfcsr_deposit_cic2d(const double *q1, const double *q2, const double *w0,
+                        const double *w1, int64_t n,
+                        int nb1, double start1, double end1,
+                        int nb2, double start2, double end2,
+                        double *out0, double *out1,
+                        void *workspace, size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Distribution-function finalisation: everything get_DF does after the two
+ * deposits (deposit.py:183-235), in place on device arrays [nx][nz]:
+ * threshold and vx = vxsum / density, Savitzky-Golay smoothing along x then
+ * z (scipy savgol_filter, mode 'interp'), trapz normalisation, numpy.gradient
+ * derivatives, smoothing of the derivatives, vx_x fill.
+ *
+ * Host-side parameter block (all pointers in `p` are DEVICE pointers):
+ */
+typedef struct {
+    int nx, nz;                 /* grid size                                  */
+    int window, order;          /* SG window (odd) and polynomial order       */
+    double velocity_threshold;  /* DF_tracker.velocity_threhold               */
+    const double *sg_coeff;     /* [window] interior coefficients             */
+    const double *sg_lo;        /* [window/2][window] left edge map           */
+    const double *sg_hi;        /* [window/2][window] right edge map          */
+    const double *gx;           /* [4][nx]: a,b,c (interior), edge 1/dx info  */
+    const double *gz;           /* [4][nz]                                    */
+    const double *dxg;          /* [nx-1] diff(x_grids)                       */
+    const double *dzg;          /* [nz-1] diff(z_grids)                       */
+    int gx_uniform, gz_uniform; /* numpy.gradient uniform-spacing path taken  */
+    double gx_dx, gz_dx;        /* the uniform spacing when taken             */
+} dfcsr_df_params;
+
+/* density, vx: in = raw deposits, out = final fields.  density_x,
+ * density_z, vx_x: outputs.  scalars_out[8] (device): 0 dsum, 1 thr,
+ * 2 thr2, 3 vx_x fill, 4 mean(vx_x), 5 max raw density, 6 max density.
+ * Scratch: dfcsr_df_workspace_bytes(nx, nz). */
+size_t dfcsr_df_workspace_bytes(int nx, int nz);
+int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, double *vx,
+                      double *density_x, double *density_z, double *vx_x,
+                      double *scalars_out, void *workspace, size_t workspace_bytes,
+                      void *stream);
+
+/* ------------------------------------------------------------------------
+ * History regrid.  Replaces DF_interp (deposit.py:296-309: scipy
+ * RegularGridInterpolator, linear, bounds_error False) for the five fields
+ * appended by append_interpolant (deposit.py:321-337, 379-390).
+ *
+ * The source fields are five device arrays [snx][snz]; the target is one
+ * slot of the device history ring.  The per-axis interval indices and
+ * normalised distances (tensor-product grids) are precomputed by the host:
+ * ix[nxi], wx[nxi], oobx[nxi] (1 = outside), iz[nzi], wz[nzi], oobz[nzi].
+ * vx_x_fill is a DEVICE pointer to the fill value of vx_x (its mean).
+ * ring64: [slot][nxi][nzi][5] doubles (or NULL); ring32: [slot][nxi][nzi][8]
+ * floats, fields 0..4 used (or NULL).  Field order: density, density_x,
+ * density_z, vx, vx_x.
+ */
+int dfcsr_history_regrid(const double *density, const double *density_x,
+                         const double *density_z, const double *vx,
+                         const double *vx_x, int snx, int snz,
+                         const int32_t *ix, const double *wx, const uint8_t *oobx, int nxi,
+                         const int32_t *iz, const double *wz, const uint8_t *oobz, int nzi,
+                         const double *vx_x_fill,
+                         double *ring64_slot, float *ring32_slot, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Standalone interpolants (API parity with the numba functions).
+ * interpolate3D (interp3D.py:18-66) on a C-order [nt][nx][nz] double grid;
+ * interpolate1D (interp1D.py:13-36).  int() truncation semantics: a query
+ * with -1 < u < 0 extrapolates from the first cell; u <= -1 or u >= n -> 0.
+ */
+int dfcsr_interp3d(const double *qt, const double *qx, const double *qz, int64_t m,
+                   const double *data, int nt, int nx, int nz,
+                   double min_t, double min_x, double min_z,
+                   double delta_t, double delta_x, double delta_z,
+                   double *out, void *stream);
+int dfcsr_interp1d(const double *q, int64_t m, const double *table, int n,
+                   double min_x, double delta_x, double *out, void *stream);
+
+/* ------------------------------------------------------------------------
+ * CSR wake.  Replaces calculate_2D_CSR / get_CSR_wake / get_CSR_integrand
+ * (CSR.py:397-418, 454-602, 605-782) for a batch of observation points.
+ *
+ * A job describes one beam's history, lattice and parameters; observation
+ * point k uses job job_of_point[k] (NULL: all use job 0).  The job array
+ * lives in DEVICE memory.
+ */
+typedef struct {
+    const double *ring64;       /* [cap][nx][nz][5] or NULL                   */
+    const float *ring32;        /* [cap][nx][nz][8] or NULL                   */
+    int cap, head, nt, nx, nz;  /* ring capacity, oldest slot, slices, grid   */
+    int pad0;
+    double t_min, x_min, z_min; /* build_interpolant (deposit.py:416-421)     */
+    double t_delta, x_delta, z_delta;
+    const double *lattice;      /* [nsample][6]: X0, Y0, nX, nY, tauX, tauY   */
+    int nsample, nelement;
+    double s_min, s_delta;      /* Lattice.build_interpolant (lattice.py:141) */
+    const double *rho;          /* [nelement] curvature angle/L               */
+    const double *distance;     /* [nelement] cumulative element ends         */
+    double position;            /* beam.position = t                          */
+    double sigma_z, sigma_x;    /* beam._sigma_z, beam._sigma_x               */
+    double slope0, mean_x;      /* beam._slope[0], beam._mean_x               */
+    double formation_length, n_formation_length;
+    double csr_scaling;         /* 8.98755e3 * charge (CSR.py:80)             */
+    int zbins, xbins;           /* Integration_params                         */
+    double near_band;           /* mixed only: |s' - s| below which the       */
+                                /* integrand runs in FP64 (0 = none)          */
+} dfcsr_wake_job;
+
+/* Plain FP64 drop-in: reproduces the reference's IEEE operation order
+ * (trapz over x' summed row by row, then numpy pairwise over s').  Needs
+ * ring64.  Outputs dE[n], xkick[n] (MeV/m). */
+int dfcsr_wake_fp64(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
+                    const double *s, const double *x, int64_t n,
+                    double *dE, double *xkick, void *stream);
+
+/* get_CSR_integrand (CSR.py:605-782) at m arbitrary points (sp[k], xp[k])
+ * for one observation point (s, x) of *job (device pointer), plain FP64.
+ * ignore_vx != 0 zeroes vx, vx_ret and vx_x_ret like the reference flag.
+ * Outputs Iz[m] (longitudinal) and Ix[m] (transverse) integrands. */
+int dfcsr_wake_integrand(const dfcsr_wake_job *job, double s, double x,
+                         const double *sp, const double *xp, int64_t m, int ignore_vx,
+                         double *Iz, double *Ix, void *stream);
+
+/* Mixed precision: FP64 per-(point, s') retarded geometry written as
+ * per-column records, FP32 gathers and integrand with history coordinates
+ * carried as integer cell + FP32 offset, Kahan-compensated FP32 sums reduced
+ * in FP64 (fixed order).  Needs ring32 in every job.  xbins_max / zbins_max
+ * bound the integration bins of all jobs in the call.  use_band != 0 runs
+ * the s' columns with |s' - s| < job.near_band through the FP64 integrand.
+ * Scratch: dfcsr_wake_workspace_bytes(xbins_max, zbins_max, n); points are
+ * processed in batches sized to keep the records resident in L2. */
+size_t dfcsr_wake_workspace_bytes(int xbins_max, int zbins_max, int64_t n);
+int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
+                     const double *s, const double *x, int64_t n,
+                     int xbins_max, int zbins_max, int use_band,
+                     double *dE, double *xkick,
+                     void *workspace, size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DFCSR_GB300_H */

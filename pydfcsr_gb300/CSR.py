@@ -1,0 +1,286 @@
+"""CSR wake on the GPU: drop-in for the wake methods of ``pyDFCSR_2D.CSR.CSR2D``.
+
+Kept call surface (pyDFCSR_2D/CSR.py): ``initialization`` (:70-81),
+``get_formation_length`` (:140-144), ``get_CSR_mesh`` (:361-394),
+``calculate_2D_CSR`` / ``calculate_2D_CSR_parallel`` (:397-451),
+``get_CSR_wake(s, x, debug)`` (:454-602) and
+``get_CSR_integrand(s, x, t, sp, xp, ignore_vx)`` (:605-782), with the same
+attributes afterwards (``dE_dct``, ``x_kick``, ``CSR_xmesh``, ``CSR_zmesh``,
+``CSR_zrange``, ``CSR_xrange_transformed``, ``CSR_scaling``).
+
+The reference builds its beam and lattice from YAML + distgen + bmadx; here
+they are passed in (a :class:`~pydfcsr_gb300.beams.Beam` and a
+:class:`~pydfcsr_gb300.lattice.Lattice` or lattice dict).  The whole
+observation mesh is one device call; ``parallel=True`` needs no MPI split on
+one GPU and runs the same path.
+
+``precision``: ``'fp64'`` - plain FP64 drop-in (bit-compatible arithmetic
+with the reference); ``'mixed'`` - FP32 bulk with FP64 retarded geometry;
+``'both'`` keeps both history rings so either can be called.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .deposit import DF_tracker
+from .lattice import Lattice
+from .params import CSR_params, Integration_params
+from .runtime import as_device_f64, default_workspace, ptr, require_cuda, stream_handle
+
+__all__ = ["CSR2D", "WakeEvaluator"]
+
+
+def wake_job(tracker, lattice, position, sigma_z, sigma_x, slope0, mean_x, formation_length,
+             n_formation_length, csr_scaling, zbins, xbins, near_band=0.0):
+    """Host ``dfcsr_wake_job`` for one beam."""
+    require_cuda()
+    tab, rho, dist = lattice.device_tables()
+    j = _lib.WakeJob()
+    jf = tracker.job_fields()
+    j.ring64 = jf["ring64"]
+    j.ring32 = jf["ring32"]
+    for k in ("cap", "head", "nt", "nx", "nz"):
+        setattr(j, k, int(jf[k]))
+    for k in ("t_min", "x_min", "z_min", "t_delta", "x_delta", "z_delta"):
+        setattr(j, k, float(jf[k]))
+    j.lattice = tab.data_ptr()
+    j.nsample = tab.shape[0]
+    j.nelement = rho.numel()
+    j.s_min = float(lattice.min_x)
+    j.s_delta = float(lattice.delta_x)
+    j.rho = rho.data_ptr()
+    j.distance = dist.data_ptr()
+    j.position = float(position)
+    j.sigma_z, j.sigma_x = float(sigma_z), float(sigma_x)
+    j.slope0, j.mean_x = float(slope0), float(mean_x)
+    j.formation_length = float(formation_length)
+    j.n_formation_length = float(n_formation_length)
+    j.csr_scaling = float(csr_scaling)
+    j.zbins, j.xbins = int(zbins), int(xbins)
+    j.near_band = float(near_band)
+    return j
+
+
+def jobs_to_device(jobs, device=None):
+    """Copy a list of WakeJob structs into one device buffer."""
+    raw = b"".join(bytes(j) for j in jobs)
+    host = torch.frombuffer(bytearray(raw), dtype=torch.uint8)
+    return host.to(device or torch.device("cuda", torch.cuda.current_device()))
+
+
+class WakeEvaluator:
+    """Runs the wake kernels over device observation points."""
+
+    def __init__(self, workspace=None):
+        self.ws = workspace or default_workspace()
+
+    def fp64(self, jobs_dev, s, x, job_of_point=None, stream=None):
+        n = s.numel()
+        dE = torch.empty(n, dtype=torch.float64, device=s.device)
+        xk = torch.empty(n, dtype=torch.float64, device=s.device)
+        _lib.call("dfcsr_wake_fp64", ptr(jobs_dev), ptr(job_of_point), ptr(s), ptr(x), n, ptr(dE),
+                  ptr(xk), stream_handle(stream))
+        return dE, xk
+
+    def mixed(self, jobs_dev, s, x, xbins_max, zbins_max, job_of_point=None, use_band=False,
+              stream=None):
+        n = s.numel()
+        dE = torch.empty(n, dtype=torch.float64, device=s.device)
+        xk = torch.empty(n, dtype=torch.float64, device=s.device)
+        need = _lib.query("dfcsr_wake_workspace_bytes", int(xbins_max), int(zbins_max), n)
+        buf = self.ws.get("wake", need)
+        _lib.call("dfcsr_wake_mixed", ptr(jobs_dev), ptr(job_of_point), ptr(s), ptr(x), n,
+                  int(xbins_max), int(zbins_max), 1 if use_band else 0, ptr(dE), ptr(xk), ptr(buf),
+                  buf.numel(), stream_handle(stream))
+        return dE, xk
+
+
+class CSR2D:
+    """The CSR wake computation of one beam, on the GPU."""
+
+    def __init__(self, input_file=None, parallel=False, *, beam=None, lattice=None,
+                 particle_deposition=None, CSR_integration=None, CSR_computation=None,
+                 precision="fp64", grid_rule="reference", near_band=0.0):
+        if input_file is not None:
+            raise NotImplementedError(
+                "YAML input files need bmadx/distgen beams; build a Beam and pass beam=, "
+                "lattice=, particle_deposition=, CSR_integration=, CSR_computation=")
+        if precision not in ("fp64", "mixed", "both"):
+            raise ValueError("precision must be 'fp64', 'mixed' or 'both'")
+        self.precision = precision
+        self.near_band = float(near_band)
+        self.beam = beam
+        self.lattice = lattice if isinstance(lattice, Lattice) or lattice is None else Lattice(lattice)
+        self.DF_tracker = DF_tracker(particle_deposition or {}, precision=precision,
+                                     grid_rule=grid_rule)
+        self.integration_params = Integration_params(CSR_integration or {})
+        self.CSR_params = CSR_params(CSR_computation or {})
+        self.formation_length = None
+        self.parallel = False
+        self.evaluator = WakeEvaluator()
+        self._jobs_dev = None
+        if beam is not None:
+            self.initialization()
+
+    # -------------------------------------------------------------- setup
+    def initialization(self):
+        """Deposit the initial beam (CSR.py:70-81)."""
+        b = self.beam
+        self.DF_tracker.get_DF(x=b.x, z=b.z, px=b.px, t=b.position)
+        self.DF_tracker.append_DF()
+        self.DF_tracker.append_interpolant(formation_length=float("inf"),
+                                           n_formation_length=self.integration_params.n_formation_length)
+        self.CSR_scaling = 8.98755e3 * b.charge
+
+    def get_formation_length(self, R, sigma_z, phi=0.0, inbend=True):
+        """(CSR.py:140-144)"""
+        if inbend:
+            self.formation_length = (24 * (R ** 2) * sigma_z) ** (1 / 3)
+        else:
+            self.formation_length = (3 * R ** 2 * phi ** 4) / (4 * (-6 * sigma_z + R * phi ** 3))
+
+    def update_history(self, formation_length=None):
+        """The per-step DF calls of CSR2D.run (CSR.py:297-307)."""
+        if formation_length is not None:
+            self.formation_length = formation_length
+        b = self.beam
+        t = self.DF_tracker
+        t.get_DF(x=b.x, z=b.z, px=b.px, t=b.position)
+        t.append_DF()
+        t.append_interpolant(formation_length=self.formation_length,
+                             n_formation_length=self.integration_params.n_formation_length)
+        t.build_interpolant()
+
+    # --------------------------------------------------------------- mesh
+    def get_CSR_mesh(self):
+        """Observation mesh in chirp-removed coordinates (CSR.py:361-394)."""
+        b = self.beam
+        p = b.slope
+        sig_x, mean_x = b.sigma_x_transform, b.mean_x_transform
+        sig_z, mean_z = b.sigma_z, b.mean_z
+        xlim, zlim = self.CSR_params.xlim, self.CSR_params.zlim
+        xbins, zbins = self.CSR_params.xbins, self.CSR_params.zbins
+        zrange = np.linspace(mean_z - zlim * sig_z, mean_z + zlim * sig_z, zbins)
+        xrange = np.linspace(mean_x - xlim * sig_x, mean_x + xlim * sig_x, xbins)
+        xmesh_t, zmesh = np.meshgrid(xrange, zrange, indexing="ij")
+        xmesh_t = xmesh_t.flatten()
+        zmesh = zmesh.flatten()
+        self.CSR_xmesh = xmesh_t + np.polyval(p, zmesh)
+        self.CSR_zmesh = zmesh
+        self.CSR_zrange = zrange
+        self.CSR_xrange_transformed = xrange
+
+    # --------------------------------------------------------------- wake
+    def _job(self, position=None):
+        b = self.beam
+        ip = self.integration_params
+        return wake_job(self.DF_tracker, self.lattice,
+                        b.position if position is None else position, b._sigma_z, b._sigma_x,
+                        b._slope[0], b._mean_x, self.formation_length, ip.n_formation_length,
+                        self.CSR_scaling, ip.zbins, ip.xbins, self.near_band)
+
+    def _wake_kind(self, precision):
+        p = precision or ("fp64" if self.precision in ("fp64", "both") else "mixed")
+        if p == "fp64" and self.DF_tracker.precision == "mixed":
+            raise ValueError("the FP64 wake needs the FP64 history (precision 'fp64' or 'both')")
+        if p == "mixed" and self.DF_tracker.precision == "fp64":
+            raise ValueError("the mixed wake needs the FP32 history (precision 'mixed' or 'both')")
+        return p
+
+    def wake_device(self, s, x, precision=None, stream=None):
+        """dE/dct and x-kick at device observation points (float64 CUDA
+        tensors) - the hot-path call."""
+        kind = self._wake_kind(precision)
+        jobs = jobs_to_device([self._job()])
+        self._jobs_dev = jobs
+        ip = self.integration_params
+        if kind == "fp64":
+            return self.evaluator.fp64(jobs, s, x, stream=stream)
+        return self.evaluator.mixed(jobs, s, x, ip.xbins, ip.zbins,
+                                    use_band=self.near_band > 0, stream=stream)
+
+    def calculate_2D_CSR(self, precision=None):
+        """Wake on the whole observation mesh (CSR.py:397-418)."""
+        s = as_device_f64(self.beam.position + self.CSR_zmesh)
+        x = as_device_f64(self.CSR_xmesh)
+        dE, xk = self.wake_device(s, x, precision)
+        shape = (self.CSR_params.xbins, self.CSR_params.zbins)
+        self.dE_dct = dE.cpu().numpy().reshape(shape)
+        self.x_kick = xk.cpu().numpy().reshape(shape)
+
+    def calculate_2D_CSR_parallel(self, precision=None):
+        """One GPU evaluates every observation point: same as calculate_2D_CSR
+        (the reference splits the mesh over MPI ranks, CSR.py:420-451)."""
+        self.calculate_2D_CSR(precision)
+
+    def _regions(self, s, x):
+        """Integration regions of get_CSR_wake (CSR.py:478-553) on the host."""
+        b = self.beam
+        t = b.position
+        sigma_z, sigma_x, tt = b._sigma_z, b._sigma_x, b._slope[0]
+        x0 = (s - t) * b._slope[0]
+        xmean = b._mean_x
+        zb, xb = self.integration_params.zbins, self.integration_params.xbins
+        nLf = self.integration_params.n_formation_length * self.formation_length
+        if np.abs(tt) <= 1:
+            s2, s3, s4 = s - 500 * sigma_z, s - 20 * sigma_z, s + 5 * sigma_z
+            s1 = np.max((0, s2 - nLf))
+            return False, [(2 * xb, zb, x0 - 20 * sigma_x, x0 + 20 * sigma_x, s1, s2),
+                           (xb, zb, x0 - 10 * sigma_x, x0 + 10 * sigma_x, s2, s3),
+                           (xb, zb, x0 - 10 * sigma_x, x0 + 10 * sigma_x, s3, s4)]
+        if tt > 0:
+            tan_alpha = -2 * tt / (1 - tt ** 2)
+            d = (10 * sigma_x + xmean - x) / tan_alpha
+            s4 = s + 3 * sigma_z
+            s3 = np.max((0, s - d))
+            s2 = s3 - 200 * sigma_z
+            x1l, x1r = x + 0.1 * sigma_x, x + 10 * sigma_x
+            x2l, x2r = x - 3 * sigma_x, x + 0.1 * sigma_x
+        else:
+            tan_alpha = 2 * tt / (1 - tt ** 2)
+            d = -(xmean - x - 10 * sigma_x) / tan_alpha
+            s4 = s + 3 * sigma_z
+            s3 = np.max((0, s - d))
+            s2 = s3 - 200 * sigma_z
+            x1l, x1r = x - 10 * sigma_x, x - 1 * sigma_x
+            x2l, x2r = x - 1 * sigma_x, x + 3 * sigma_x
+        s1 = np.max((0, s2 - nLf))
+        return True, [(2 * xb, zb, x0 - 20 * sigma_x, x0 + 20 * sigma_x, s1, s2),
+                      (xb, zb, x0 - 5 * sigma_x, x0 + 5 * sigma_x, s2, s3),
+                      (xb, zb, x1l, x1r, s3, s4),
+                      (xb, zb, x2l, x2r, s3, s4)]
+
+    def get_CSR_wake(self, s, x, debug=False):
+        """Wake at one observation point (CSR.py:454-602).  ``debug=True``
+        returns the reference's tuple of region grids and integrand arrays."""
+        if not debug:
+            dE, xk = self.wake_device(as_device_f64([s]), as_device_f64([x]))
+            dE, xk = dE.cpu().numpy(), xk.cpu().numpy()
+            return float(dE[0]), float(xk[0])
+        chirp, regs = self._regions(s, x)
+        xps, sps, ints = [], [], []
+        for (nxp, nsp, xl, xr, sl, sr) in regs:
+            xp = np.linspace(xl, xr, nxp)
+            sp = np.linspace(sl, sr, nsp)
+            xpm, spm = np.meshgrid(xp, sp, indexing="ij")
+            Iz, Ix = self.get_CSR_integrand(s=s, x=x, t=self.beam.position, sp=spm, xp=xpm)
+            xps.append(xp); sps.append(sp); ints += [Iz, Ix]
+        if chirp:
+            # xp1, xp2, xp3, xp4, sp1, sp2, sp3, then the integrands per region
+            return (xps[2], xps[3], xps[1], xps[0], sps[0], sps[1], sps[2], *ints)
+        return (xps[0], xps[1], sps[0], sps[1], sps[2], *ints)
+
+    def get_CSR_integrand(self, s, x, t, sp, xp, ignore_vx=False):
+        """FP64 integrands at the mesh (sp, xp) (CSR.py:605-782)."""
+        spd = as_device_f64(np.asarray(sp)).reshape(-1)
+        xpd = as_device_f64(np.asarray(xp)).reshape(-1)
+        jobs = jobs_to_device([self._job(position=t)])
+        m = spd.numel()
+        Iz = torch.empty(m, dtype=torch.float64, device=spd.device)
+        Ix = torch.empty(m, dtype=torch.float64, device=spd.device)
+        _lib.call("dfcsr_wake_integrand", ptr(jobs), float(s), float(x), ptr(spd), ptr(xpd), m,
+                  1 if ignore_vx else 0, ptr(Iz), ptr(Ix), stream_handle())
+        shape = np.shape(xp)
+        return Iz.cpu().numpy().reshape(shape), Ix.cpu().numpy().reshape(shape)

@@ -1,0 +1,169 @@
+"""ctypes binding of ``libdfcsr_gb300.so`` (the C ABI in include/dfcsr_gb300.h).
+
+Loading never falls back to anything: if the shared library is missing and
+cannot be built, importing a compute entry point raises.  Status codes become
+Python exceptions with the library's thread-local message.
+"""
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_c_double = ctypes.c_double
+_c_int = ctypes.c_int
+_c_i64 = ctypes.c_int64
+_c_size = ctypes.c_size_t
+_p = ctypes.c_void_p
+
+
+class DfcsrError(RuntimeError):
+    """A dfcsr_gb300 C-ABI call failed."""
+
+    def __init__(self, status, name, message):
+        super().__init__(f"{name}: [{status_name(status)}] {message}")
+        self.status = status
+
+
+class DfcsrBadArgument(DfcsrError, ValueError):
+    pass
+
+
+class DfcsrOutOfMemory(DfcsrError, MemoryError):
+    pass
+
+
+class DfcsrTimeout(DfcsrError, TimeoutError):
+    pass
+
+
+class DfcsrKernelError(DfcsrError):
+    pass
+
+
+class DfcsrCudaError(DfcsrError):
+    pass
+
+
+class DfcsrAdmissionRefused(DfcsrError):
+    pass
+
+
+_EXC = {1: DfcsrBadArgument, 2: DfcsrOutOfMemory, 3: DfcsrTimeout, 4: DfcsrKernelError,
+        5: DfcsrCudaError, 6: DfcsrAdmissionRefused}
+
+_NAMES = {0: "OK", 1: "BAD_ARG", 2: "OOM", 3: "TIMEOUT", 4: "KERNEL_ERROR", 5: "CUDA_ERROR",
+          6: "ADMISSION_REFUSED"}
+
+
+def status_name(status):
+    return _NAMES.get(status, "UNKNOWN")
+
+
+class DFParams(ctypes.Structure):
+    """``dfcsr_df_params``."""
+    _fields_ = [
+        ("nx", _c_int), ("nz", _c_int), ("window", _c_int), ("order", _c_int),
+        ("velocity_threshold", _c_double),
+        ("sg_coeff", _p), ("sg_lo", _p), ("sg_hi", _p), ("gx", _p), ("gz", _p),
+        ("dxg", _p), ("dzg", _p),
+        ("gx_uniform", _c_int), ("gz_uniform", _c_int),
+        ("gx_dx", _c_double), ("gz_dx", _c_double),
+    ]
+
+
+class WakeJob(ctypes.Structure):
+    """``dfcsr_wake_job``."""
+    _fields_ = [
+        ("ring64", _p), ("ring32", _p),
+        ("cap", _c_int), ("head", _c_int), ("nt", _c_int), ("nx", _c_int), ("nz", _c_int),
+        ("pad0", _c_int),
+        ("t_min", _c_double), ("x_min", _c_double), ("z_min", _c_double),
+        ("t_delta", _c_double), ("x_delta", _c_double), ("z_delta", _c_double),
+        ("lattice", _p), ("nsample", _c_int), ("nelement", _c_int),
+        ("s_min", _c_double), ("s_delta", _c_double),
+        ("rho", _p), ("distance", _p),
+        ("position", _c_double), ("sigma_z", _c_double), ("sigma_x", _c_double),
+        ("slope0", _c_double), ("mean_x", _c_double),
+        ("formation_length", _c_double), ("n_formation_length", _c_double),
+        ("csr_scaling", _c_double),
+        ("zbins", _c_int), ("xbins", _c_int),
+        ("near_band", _c_double),
+    ]
+
+
+# (name, restype, argtypes)
+_SIGS = [
+    ("dfcsr_version", _c_int, []),
+    ("dfcsr_last_error", ctypes.c_char_p, []),
+    ("dfcsr_status_name", ctypes.c_char_p, [_c_int]),
+    ("dfcsr_abi_sizeof", _c_size, [_c_int]),
+    ("dfcsr_moments_workspace_bytes", _c_size, [_c_i64]),
+    ("dfcsr_beam_moments", _c_int, [_p, _p, _c_i64, _p, _p, _c_size, _p]),
+    ("dfcsr_deposit_workspace_bytes", _c_size, [_c_i64, _c_int, _c_int]),
+    ("dfcsr_deposit_cic2d", _c_int, [_p, _p, _p, _p, _c_i64, _c_int, _c_double, _c_double,
+                                      _c_int, _c_double, _c_double, _p, _p, _p, _c_size, _p]),
+    ("dfcsr_df_workspace_bytes", _c_size, [_c_int, _c_int]),
+    ("dfcsr_df_finalize", _c_int, [ctypes.POINTER(DFParams), _p, _p, _p, _p, _p, _p, _p,
+                                    _c_size, _p]),
+    ("dfcsr_history_regrid", _c_int, [_p, _p, _p, _p, _p, _c_int, _c_int, _p, _p, _p, _c_int,
+                                       _p, _p, _p, _c_int, _p, _p, _p, _p]),
+    ("dfcsr_interp3d", _c_int, [_p, _p, _p, _c_i64, _p, _c_int, _c_int, _c_int, _c_double,
+                                 _c_double, _c_double, _c_double, _c_double, _c_double, _p, _p]),
+    ("dfcsr_interp1d", _c_int, [_p, _c_i64, _p, _c_int, _c_double, _c_double, _p, _p]),
+    ("dfcsr_wake_fp64", _c_int, [_p, _p, _p, _p, _c_i64, _p, _p, _p]),
+    ("dfcsr_wake_integrand", _c_int, [_p, _c_double, _c_double, _p, _p, _c_i64, _c_int, _p, _p,
+                                       _p]),
+    ("dfcsr_wake_workspace_bytes", _c_size, [_c_int, _c_int, _c_i64]),
+    ("dfcsr_wake_mixed", _c_int, [_p, _p, _p, _p, _c_i64, _c_int, _c_int, _c_int, _p, _p, _p,
+                                   _c_size, _p]),
+]
+
+EXPORTS = [n for n, _, _ in _SIGS]
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_needed=True):
+    """Load (building first if the sources are newer) and return the CDLL."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_needed and not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(path):
+            raise ImportError(f"dfcsr_gb300 native library not found at {path}; run "
+                              "`python -m pydfcsr_gb300.build` (needs nvcc for sm_103a)")
+        lib = ctypes.CDLL(path)
+        for name, res, args in _SIGS:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if lib.dfcsr_abi_sizeof(0) != ctypes.sizeof(DFParams):
+            raise ImportError("dfcsr_df_params layout mismatch between binding and library")
+        if lib.dfcsr_abi_sizeof(1) != ctypes.sizeof(WakeJob):
+            raise ImportError("dfcsr_wake_job layout mismatch between binding and library")
+        _lib = lib
+        return lib
+
+
+def call(name, *args):
+    """Call an entry point and raise the matching exception on failure."""
+    lib = load()
+    st = getattr(lib, name)(*args)
+    if st != 0:
+        msg = lib.dfcsr_last_error().decode(errors="replace")
+        raise _EXC.get(st, DfcsrError)(st, name, msg)
+    return st
+
+
+def query(name, *args):
+    """Call a size / info function (no status)."""
+    return getattr(load(), name)(*args)

@@ -1,0 +1,448 @@
+// Beam moments and the deterministic cloud-in-cell deposit.
+//
+// histogram_cic_2d (pyDFCSR_2D/deposit.py:43-87) scatters four corner weights
+// per particle serially.  Here particles are sorted by their lower cell with
+// a stable LSD radix sort (8-bit digits, per-warp match_any ranking, no
+// atomics), every lower cell is reduced by one warp in a fixed order into
+// eight partial sums (4 corners x 2 weight channels), and a gather pass adds
+// the four partials that land on each output cell.  Same result for the same
+// input on every run; no floating-point atomics anywhere.
+#include "dfcsr_common.cuh"
+
+namespace dfcsr {
+
+// ------------------------------------------------------------------ moments
+constexpr int MOM_THREADS = 256;
+constexpr int MOM_MAX_BLOCKS = 1024;
+constexpr int MOM_K = 4;   // partial sums per pass
+
+static int moment_blocks(int64_t n) {
+    int64_t b = (n + MOM_THREADS * 8 - 1) / (MOM_THREADS * 8);
+    if (b < 1) b = 1;
+    if (b > MOM_MAX_BLOCKS) b = MOM_MAX_BLOCKS;
+    return (int)b;
+}
+
+// stats layout (see header): 0 n, 1 mean_x, 2 mean_z, 3 sigma_x, 4 sigma_z,
+// 5 slope, 6 intercept, 7 n_slice, 8 sigma_x_slice, 9 mean_xt, 10 sigma_xt,
+// 11 cov_xz, 12 slice mean (internal), 13 sum_xx, 14 sum_zz, 15 sum_xz
+template <int PASS>
+__global__ void __launch_bounds__(MOM_THREADS)
+moments_pass(const double *__restrict__ x, const double *__restrict__ z, int64_t n,
+             const double *__restrict__ stats, double *__restrict__ partial) {
+    __shared__ double red[MOM_THREADS / 32];
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    double mx = 0, mz = 0, sz = 0, slope = 0, icpt = 0, ms = 0, mt = 0;
+    if (PASS >= 2) { mx = stats[1]; mz = stats[2]; }
+    if (PASS >= 3) { sz = stats[4]; slope = stats[5]; icpt = stats[6]; }
+    if (PASS >= 4) { ms = stats[12]; mt = stats[9]; }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double xi = x[i], zi = z[i];
+        if (PASS == 1) {
+            a0 += xi;
+            a1 += zi;
+        } else if (PASS == 2) {
+            const double dx = xi - mx, dz = zi - mz;
+            a0 += dx * dx;
+            a1 += dz * dz;
+            a2 += dx * dz;
+        } else if (PASS == 3) {
+            if (fabs(zi) < 0.1 * sz) { a0 += 1.0; a1 += xi; }
+            a2 += xi - (slope * zi + icpt);
+        } else {
+            if (fabs(zi) < 0.1 * sz) { const double d = xi - ms; a0 += d * d; }
+            const double dt = (xi - (slope * zi + icpt)) - mt;
+            a1 += dt * dt;
+        }
+    }
+    double v[MOM_K] = {a0, a1, a2, a3};
+    for (int k = 0; k < MOM_K; ++k) {
+        const double s = block_sum(v[k], red);
+        if (threadIdx.x == 0) partial[(size_t)blockIdx.x * MOM_K + k] = s;
+    }
+}
+
+template <int PASS>
+__global__ void __launch_bounds__(MOM_THREADS)
+moments_finish(const double *__restrict__ partial, int nblk, int64_t n, double *__restrict__ stats) {
+    __shared__ double red[MOM_THREADS / 32];
+    double tot[MOM_K];
+    for (int k = 0; k < MOM_K; ++k) {
+        double a = 0;
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x) a += partial[(size_t)b * MOM_K + k];
+        tot[k] = block_sum(a, red);
+    }
+    if (threadIdx.x != 0) return;
+    const double dn = (double)n;
+    if (PASS == 1) {
+        stats[0] = dn;
+        stats[1] = tot[0] / dn;
+        stats[2] = tot[1] / dn;
+    } else if (PASS == 2) {
+        stats[13] = tot[0]; stats[14] = tot[1]; stats[15] = tot[2];
+        stats[3] = sqrt(tot[0] / dn);
+        stats[4] = sqrt(tot[1] / dn);
+        stats[11] = tot[2] / dn;
+        const double slope = tot[2] / tot[1];
+        stats[5] = slope;
+        stats[6] = stats[1] - slope * stats[2];
+    } else if (PASS == 3) {
+        stats[7] = tot[0];
+        stats[12] = tot[1] / tot[0];          // NaN when the slice is empty
+        stats[9] = tot[2] / dn;
+    } else {
+        stats[8] = sqrt(tot[0] / stats[7]);   // NaN when the slice is empty
+        stats[10] = sqrt(tot[1] / dn);
+    }
+}
+
+// ----------------------------------------------------------------- CIC keys
+// Lower-cell key of a particle: (i1 + 1) * (nb2 + 1) + (i2 + 1) for
+// i1 in [-1, nb1 - 1], i2 in [-1, nb2 - 1]; particles with no corner inside
+// the grid get the sentinel nkeys and sort to the end.
+__global__ void cic_keys(const double *__restrict__ q1, const double *__restrict__ q2, int64_t n,
+                         int nb1, double start1, double inv1, int nb2, double start2, double inv2,
+                         uint32_t nkeys, uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double c1 = __dmul_rn(__dsub_rn(q1[i], start1), inv1);
+    const double c2 = __dmul_rn(__dsub_rn(q2[i], start2), inv2);
+    const double f1 = floor(c1), f2 = floor(c2);
+    uint32_t key = nkeys;
+    if (f1 > -2.0 && f1 < (double)nb1 && f2 > -2.0 && f2 < (double)nb2) {
+        const int i1 = (int)f1, i2 = (int)f2;
+        key = (uint32_t)(i1 + 1) * (uint32_t)(nb2 + 1) + (uint32_t)(i2 + 1);
+    }
+    keys[i] = key;
+    vals[i] = (uint32_t)i;
+}
+
+// ------------------------------------------------------------- radix sort
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_BINS = 256;
+
+__global__ void __launch_bounds__(RS_THREADS)
+radix_upsweep(const uint32_t *__restrict__ keys, int64_t n, int shift, int ntiles,
+              uint32_t *__restrict__ hist) {
+    __shared__ uint32_t cnt[RS_BINS];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * RS_TILE;
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const int64_t idx = base + (int64_t)r * RS_THREADS + threadIdx.x;
+        if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & 255u], 1u);   // integer: exact
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// One block per digit: exclusive scan of hist[digit][0..ntiles) in place,
+// row total to dtot[digit].
+__global__ void __launch_bounds__(1024)
+radix_scan_rows(uint32_t *__restrict__ hist, int ntiles, uint32_t *__restrict__ dtot) {
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry_s;
+    uint32_t *row = hist + (size_t)blockIdx.x * ntiles;
+    if (threadIdx.x == 0) carry_s = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 0; off < ntiles; off += 1024) {
+        const int i = off + threadIdx.x;
+        const uint32_t v = (i < ntiles) ? row[i] : 0u;
+        uint32_t inc = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = wsum[lane];
+            uint32_t winc = w;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, winc, o);
+                if (lane >= o) winc += t;
+            }
+            wsum[lane] = winc - w;   // exclusive warp offsets
+        }
+        __syncthreads();
+        const uint32_t carry = carry_s;
+        if (i < ntiles) row[i] = carry + wsum[warp] + inc - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry_s = carry + wsum[warp] + inc;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) dtot[blockIdx.x] = carry_s;
+}
+
+__global__ void __launch_bounds__(RS_THREADS)
+radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, int64_t n,
+              int shift, int ntiles, const uint32_t *__restrict__ hist,
+              const uint32_t *__restrict__ dtot, uint32_t *__restrict__ keys_out,
+              uint32_t *__restrict__ vals_out) {
+    __shared__ uint32_t wcnt[RS_WARPS][RS_BINS];
+    __shared__ uint32_t dbase[RS_BINS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int d = threadIdx.x; d < RS_WARPS * RS_BINS; d += RS_THREADS) (&wcnt[0][0])[d] = 0;
+    if (warp == 0) {
+        // exclusive scan of the 256 digit totals (8 per lane)
+        uint32_t loc[8], s = 0;
+        for (int k = 0; k < 8; ++k) { loc[k] = dtot[lane * 8 + k]; s += loc[k]; }
+        uint32_t inc = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        uint32_t run = inc - s;
+        for (int k = 0; k < 8; ++k) { dbase[lane * 8 + k] = run; run += loc[k]; }
+    }
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)warp * (32 * RS_ITEMS);
+    uint32_t k[RS_ITEMS], v[RS_ITEMS], rank[RS_ITEMS];
+    int dig[RS_ITEMS];
+    const unsigned lt_mask = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const int64_t idx = base + r * 32 + lane;
+        const bool valid = idx < n;
+        const uint32_t key = valid ? keys[idx] : 0u;
+        const int d = valid ? (int)((key >> shift) & 255u) : RS_BINS;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int leader = __ffs(peers) - 1;
+        uint32_t before = 0;
+        if (valid) before = wcnt[warp][d];
+        __syncwarp();
+        if (valid && lane == leader) wcnt[warp][d] = before + __popc(peers);
+        __syncwarp();
+        rank[r] = before + __popc(peers & lt_mask);
+        dig[r] = d;
+        k[r] = key;
+        v[r] = valid ? vals[idx] : 0u;
+    }
+    __syncthreads();
+    {
+        const int d = threadIdx.x;   // RS_THREADS == RS_BINS
+        uint32_t run = 0;
+        for (int w = 0; w < RS_WARPS; ++w) {
+            const uint32_t t = wcnt[w][d];
+            wcnt[w][d] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const int d = dig[r];
+        if (d < RS_BINS) {
+            const uint32_t pos = dbase[d] + hist[(size_t)d * ntiles + blockIdx.x] + wcnt[warp][d] + rank[r];
+            keys_out[pos] = k[r];
+            vals_out[pos] = v[r];
+        }
+    }
+}
+
+// ------------------------------------------------------------- cell sums
+__global__ void cell_ranges(const uint32_t *__restrict__ keys, int64_t n,
+                            uint32_t *__restrict__ cstart, uint32_t *__restrict__ cend) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = keys[i];
+    if (i == 0 || keys[i - 1] != k) cstart[k] = (uint32_t)i;
+    if (i == n - 1 || keys[i + 1] != k) cend[k] = (uint32_t)(i + 1);
+}
+
+// One warp per lower cell: eight partial sums (corners 00, 01, 10, 11 for
+// channel 0 then channel 1), lanes stride through the cell's particles in
+// sorted (= original) order, then a fixed xor-shuffle tree.
+__global__ void __launch_bounds__(256)
+cell_sums(const uint32_t *__restrict__ vals, const uint32_t *__restrict__ cstart,
+          const uint32_t *__restrict__ cend, uint32_t nkeys, int nb2,
+          const double *__restrict__ q1, const double *__restrict__ q2,
+          const double *__restrict__ w0, const double *__restrict__ w1,
+          double start1, double inv1, double start2, double inv2,
+          double *__restrict__ partial) {
+    const uint32_t key = (uint32_t)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (key >= nkeys) return;
+    const int i1 = (int)(key / (uint32_t)(nb2 + 1)) - 1;
+    const int i2 = (int)(key % (uint32_t)(nb2 + 1)) - 1;
+    const uint32_t b = cstart[key], e = cend[key];
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t p = b + lane; p < e; p += 32) {
+        const uint32_t idx = vals[p];
+        const double c1 = __dmul_rn(__dsub_rn(q1[idx], start1), inv1);
+        const double c2 = __dmul_rn(__dsub_rn(q2[idx], start2), inv2);
+        const double s1 = __dsub_rn(1.0, __dsub_rn(c1, (double)i1));
+        const double s2 = __dsub_rn(1.0, __dsub_rn(c2, (double)i2));
+        const double t1 = __dsub_rn(1.0, s1), t2 = __dsub_rn(1.0, s2);
+        const double wa = w0 ? w0[idx] : 1.0;
+        acc[0] = __dadd_rn(acc[0], __dmul_rn(__dmul_rn(wa, s1), s2));
+        acc[1] = __dadd_rn(acc[1], __dmul_rn(__dmul_rn(wa, s1), t2));
+        acc[2] = __dadd_rn(acc[2], __dmul_rn(__dmul_rn(wa, t1), s2));
+        acc[3] = __dadd_rn(acc[3], __dmul_rn(__dmul_rn(wa, t1), t2));
+        if (w1) {
+            const double wb = w1[idx];
+            acc[4] = __dadd_rn(acc[4], __dmul_rn(__dmul_rn(wb, s1), s2));
+            acc[5] = __dadd_rn(acc[5], __dmul_rn(__dmul_rn(wb, s1), t2));
+            acc[6] = __dadd_rn(acc[6], __dmul_rn(__dmul_rn(wb, t1), s2));
+            acc[7] = __dadd_rn(acc[7], __dmul_rn(__dmul_rn(wb, t1), t2));
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+        for (int o = 16; o > 0; o >>= 1) acc[c] = __dadd_rn(acc[c], __shfl_xor_sync(0xffffffffu, acc[c], o));
+    if (lane < 8) partial[(size_t)key * 8 + lane] = acc[lane];
+}
+
+__global__ void cic_assemble(const double *__restrict__ partial, int nb1, int nb2,
+                             double *__restrict__ out0, double *__restrict__ out1) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nb1 * nb2) return;
+    const int a = (int)(t / nb2), b = (int)(t % nb2);
+    const int W = nb2 + 1;
+    // key of lower cell (i1, i2) = (i1 + 1) * W + (i2 + 1)
+    const size_t k00 = (size_t)(a + 1) * W + (b + 1);   // this cell as lower corner
+    const size_t k01 = (size_t)(a + 1) * W + b;         // (a, b-1) -> its corner 01
+    const size_t k10 = (size_t)a * W + (b + 1);         // (a-1, b) -> its corner 10
+    const size_t k11 = (size_t)a * W + b;               // (a-1, b-1) -> its corner 11
+    out0[t] = __dadd_rn(__dadd_rn(__dadd_rn(partial[k00 * 8 + 0], partial[k01 * 8 + 1]),
+                                  partial[k10 * 8 + 2]), partial[k11 * 8 + 3]);
+    if (out1)
+        out1[t] = __dadd_rn(__dadd_rn(__dadd_rn(partial[k00 * 8 + 4], partial[k01 * 8 + 5]),
+                                      partial[k10 * 8 + 6]), partial[k11 * 8 + 7]);
+}
+
+struct DepositLayout {
+    uint32_t nkeys;
+    int bits, passes, ntiles;
+};
+
+static DepositLayout deposit_layout(int64_t n, int nb1, int nb2) {
+    DepositLayout L;
+    L.nkeys = (uint32_t)(nb1 + 1) * (uint32_t)(nb2 + 1);
+    int bits = 1;
+    while ((1ull << bits) <= (unsigned long long)L.nkeys) ++bits;   // sentinel included
+    L.bits = bits;
+    L.passes = (bits + 7) / 8;
+    L.ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
+    if (L.ntiles < 1) L.ntiles = 1;
+    return L;
+}
+
+static size_t deposit_carve(Carver &c, int64_t n, const DepositLayout &L, uint32_t **ka,
+                            uint32_t **va, uint32_t **kb, uint32_t **vb, uint32_t **hist,
+                            uint32_t **dtot, uint32_t **cs, uint32_t **ce, double **part) {
+    const size_t nn = (size_t)(n > 0 ? n : 1);
+    *ka = c.take<uint32_t>(nn);
+    *va = c.take<uint32_t>(nn);
+    *kb = c.take<uint32_t>(nn);
+    *vb = c.take<uint32_t>(nn);
+    *hist = c.take<uint32_t>((size_t)RS_BINS * L.ntiles);
+    *dtot = c.take<uint32_t>(RS_BINS);
+    *cs = c.take<uint32_t>((size_t)L.nkeys + 1);
+    *ce = c.take<uint32_t>((size_t)L.nkeys + 1);
+    *part = c.take<double>((size_t)L.nkeys * 8);
+    return c.used;
+}
+
+}  // namespace dfcsr
+
+using namespace dfcsr;
+
+extern "C" size_t dfcsr_moments_workspace_bytes(int64_t n) {
+    return align_up((size_t)moment_blocks(n) * MOM_K * sizeof(double), 256) + 256;
+}
+
+extern "C" int dfcsr_beam_moments(const double *x, const double *z, int64_t n, double *out,
+                                  void *workspace, size_t workspace_bytes, void *stream) {
+    clear_error();
+    DFCSR_CHECK_ARG(x && z && out, "dfcsr_beam_moments: null pointer");
+    DFCSR_CHECK_ARG(n > 0, "dfcsr_beam_moments: n must be positive (got %lld)", (long long)n);
+    const int nblk = moment_blocks(n);
+    if (!workspace || workspace_bytes < dfcsr_moments_workspace_bytes(n)) {
+        set_error("dfcsr_beam_moments: workspace too small (%zu < %zu)", workspace_bytes,
+                  dfcsr_moments_workspace_bytes(n));
+        return DFCSR_OOM;
+    }
+    cudaStream_t s = as_stream(stream);
+    double *part = reinterpret_cast<double *>(workspace);
+    DFCSR_CUDA_TRY(cudaMemsetAsync(out, 0, 16 * sizeof(double), s));
+    moments_pass<1><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
+    moments_finish<1><<<1, MOM_THREADS, 0, s>>>(part, nblk, n, out);
+    moments_pass<2><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
+    moments_finish<2><<<1, MOM_THREADS, 0, s>>>(part, nblk, n, out);
+    moments_pass<3><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
+    moments_finish<3><<<1, MOM_THREADS, 0, s>>>(part, nblk, n, out);
+    moments_pass<4><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
+    moments_finish<4><<<1, MOM_THREADS, 0, s>>>(part, nblk, n, out);
+    DFCSR_LAUNCH_CHECK();
+    return DFCSR_OK;
+}
+
+extern "C" size_t dfcsr_deposit_workspace_bytes(int64_t n, int nb1, int nb2) {
+    if (n < 0 || nb1 <= 0 || nb2 <= 0) return 0;
+    const DepositLayout L = deposit_layout(n, nb1, nb2);
+    Carver c{nullptr, 0, 0};
+    uint32_t *a, *b, *cc, *d, *e, *f, *g, *h;
+    double *p;
+    return deposit_carve(c, n, L, &a, &b, &cc, &d, &e, &f, &g, &h, &p) + 256;
+}
+
+extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const double *w0,
+                                   const double *w1, int64_t n, int nb1, double start1,
+                                   double end1, int nb2, double start2, double end2,
+                                   double *out0, double *out1, void *workspace,
+                                   size_t workspace_bytes, void *stream) {
+    clear_error();
+    DFCSR_CHECK_ARG(out0, "dfcsr_deposit_cic2d: out0 is null");
+    DFCSR_CHECK_ARG(nb1 > 0 && nb2 > 0, "dfcsr_deposit_cic2d: bins must be positive (%d, %d)", nb1, nb2);
+    DFCSR_CHECK_ARG((int64_t)(nb1 + 1) * (nb2 + 1) < (1ll << 30),
+                    "dfcsr_deposit_cic2d: grid %d x %d too large", nb1, nb2);
+    DFCSR_CHECK_ARG(n >= 0 && n < (1ll << 32) - 1, "dfcsr_deposit_cic2d: bad particle count %lld",
+                    (long long)n);
+    DFCSR_CHECK_ARG(n == 0 || (q1 && q2), "dfcsr_deposit_cic2d: null coordinates");
+    DFCSR_CHECK_ARG(end1 != start1 && end2 != start2, "dfcsr_deposit_cic2d: empty bin range");
+    cudaStream_t s = as_stream(stream);
+    const DepositLayout L = deposit_layout(n, nb1, nb2);
+    Carver c{reinterpret_cast<char *>(workspace), workspace_bytes, 0};
+    uint32_t *ka, *va, *kb, *vb, *hist, *dtot, *cs, *ce;
+    double *part;
+    deposit_carve(c, n, L, &ka, &va, &kb, &vb, &hist, &dtot, &cs, &ce, &part);
+    if (!workspace || !c.ok()) {
+        set_error("dfcsr_deposit_cic2d: workspace too small (%zu < %zu)", workspace_bytes, c.used);
+        return DFCSR_OOM;
+    }
+    const double inv1 = 1.0 / ((end1 - start1) / nb1);
+    const double inv2 = 1.0 / ((end2 - start2) / nb2);
+    DFCSR_CUDA_TRY(cudaMemsetAsync(cs, 0, sizeof(uint32_t) * ((size_t)L.nkeys + 1), s));
+    DFCSR_CUDA_TRY(cudaMemsetAsync(ce, 0, sizeof(uint32_t) * ((size_t)L.nkeys + 1), s));
+    if (n > 0) {
+        const int tb = 256;
+        cic_keys<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(q1, q2, n, nb1, start1, inv1, nb2,
+                                                              start2, inv2, L.nkeys, ka, va);
+        uint32_t *kin = ka, *vin = va, *kout = kb, *vout = vb;
+        for (int p = 0; p < L.passes; ++p) {
+            const int shift = 8 * p;
+            radix_upsweep<<<L.ntiles, RS_THREADS, 0, s>>>(kin, n, shift, L.ntiles, hist);
+            radix_scan_rows<<<RS_BINS, 1024, 0, s>>>(hist, L.ntiles, dtot);
+            radix_scatter<<<L.ntiles, RS_THREADS, 0, s>>>(kin, vin, n, shift, L.ntiles, hist, dtot,
+                                                          kout, vout);
+            uint32_t *t = kin; kin = kout; kout = t;
+            t = vin; vin = vout; vout = t;
+        }
+        cell_ranges<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(kin, n, cs, ce);
+        const int64_t threads = (int64_t)L.nkeys * 32;
+        cell_sums<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+            vin, cs, ce, L.nkeys, nb2, q1, q2, w0, w1, start1, inv1, start2, inv2, part);
+    } else {
+        DFCSR_CUDA_TRY(cudaMemsetAsync(part, 0, sizeof(double) * (size_t)L.nkeys * 8, s));
+    }
+    const int64_t cells = (int64_t)nb1 * nb2;
+    cic_assemble<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(part, nb1, nb2, out0, w1 ? out1 : nullptr);
+    DFCSR_LAUNCH_CHECK();
+    return DFCSR_OK;
+}

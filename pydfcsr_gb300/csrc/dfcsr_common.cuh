@@ -1,0 +1,129 @@
+// Shared helpers of the dfcsr_gb300 CUDA library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/dfcsr_gb300.h"
+
+namespace dfcsr {
+
+// ---------------------------------------------------------------- errors
+// Thread-local message of the last failing call (defined in capi.cu).
+void set_error(const char *fmt, ...);
+void clear_error();
+
+#define DFCSR_CHECK_ARG(cond, ...)                  \
+    do {                                            \
+        if (!(cond)) {                              \
+            ::dfcsr::set_error(__VA_ARGS__);        \
+            return DFCSR_BAD_ARG;                   \
+        }                                           \
+    } while (0)
+
+#define DFCSR_CUDA_TRY(expr)                                                     \
+    do {                                                                         \
+        cudaError_t e_ = (expr);                                                 \
+        if (e_ != cudaSuccess) {                                                 \
+            ::dfcsr::set_error("%s failed: %s", #expr, cudaGetErrorString(e_));  \
+            return DFCSR_CUDA_ERROR;                                             \
+        }                                                                        \
+    } while (0)
+
+#define DFCSR_LAUNCH_CHECK()                                                     \
+    do {                                                                         \
+        cudaError_t e_ = cudaGetLastError();                                     \
+        if (e_ != cudaSuccess) {                                                 \
+            ::dfcsr::set_error("kernel launch failed: %s", cudaGetErrorString(e_)); \
+            return DFCSR_CUDA_ERROR;                                             \
+        }                                                                        \
+    } while (0)
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Carve typed sub-buffers out of a caller-provided workspace.
+struct Carver {
+    char *base;
+    size_t size, used;
+    template <class T>
+    T *take(size_t count) {
+        used = align_up(used, 256);
+        T *p = reinterpret_cast<T *>(base + used);
+        used += count * sizeof(T);
+        return p;
+    }
+    bool ok() const { return used <= size; }
+};
+
+int num_sms();
+
+// ------------------------------------------------------------ device math
+// Reference axis rule of interpolate3D / interpolate1D: i0 = int(u)
+// (truncation toward zero), i1 = i0 unless i0 is the last index, in range iff
+// -1 < u < n.  Returns false when out of range.
+__device__ __forceinline__ bool axis_index(double u, int n, int &i0, int &i1, double &frac) {
+    if (!(u > -1.0 && u < (double)n)) return false;
+    int a = (int)u;  // truncates toward zero
+    i0 = a;
+    i1 = (a == n - 1) ? a : a + 1;
+    frac = __dsub_rn(u, (double)a);
+    return true;
+}
+
+// numpy.linspace element i of linspace(start, stop, num): i*step + start,
+// last element exactly stop, step == 0 handled like numpy.
+__device__ __forceinline__ double np_linspace_at(double start, double stop, int num, int i) {
+    if (num == 1) return start;
+    if (i == num - 1) return stop;
+    const int div = num - 1;
+    const double delta = __dsub_rn(stop, start);
+    const double step = __ddiv_rn(delta, (double)div);
+    if (step == 0.0) return __dadd_rn(__dmul_rn(__ddiv_rn((double)i, (double)div), delta), start);
+    return __dadd_rn(__dmul_rn((double)i, step), start);
+}
+
+// numpy pairwise summation (PW_BLOCKSIZE 128, 8 partial accumulators).
+__device__ inline double np_pairwise(const double *a, int n) {
+    if (n < 8) {
+        double r = (n > 0) ? a[0] : 0.0;
+        for (int i = 1; i < n; ++i) r = __dadd_rn(r, a[i]);
+        return r;
+    }
+    if (n <= 128) {
+        double r[8];
+        for (int k = 0; k < 8; ++k) r[k] = a[k];
+        int i;
+        for (i = 8; i < n - (n % 8); i += 8)
+            for (int k = 0; k < 8; ++k) r[k] = __dadd_rn(r[k], a[i + k]);
+        double res = __dadd_rn(__dadd_rn(__dadd_rn(r[0], r[1]), __dadd_rn(r[2], r[3])),
+                               __dadd_rn(__dadd_rn(r[4], r[5]), __dadd_rn(r[6], r[7])));
+        for (; i < n; ++i) res = __dadd_rn(res, a[i]);
+        return res;
+    }
+    // split in halves (multiple of 8) and recurse, as numpy does
+    int n2 = n / 2;
+    n2 -= n2 % 8;
+    return __dadd_rn(np_pairwise(a, n2), np_pairwise(a + n2, n - n2));
+}
+
+// Deterministic block reduction of a double (fixed shuffle tree + fixed
+// warp order).  `red` must hold blockDim.x / 32 doubles.  Result valid in
+// thread 0.
+__device__ inline double block_sum(double v, double *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        r = red[0];
+        for (int w = 1; w < nw; ++w) r += red[w];
+    }
+    __syncthreads();
+    return r;
+}
+
+}  // namespace dfcsr

@@ -1,0 +1,88 @@
+// History ring regrid: the device side of DF_interp / append_interpolant
+// (pyDFCSR_2D/deposit.py:296-392).
+//
+// scipy RegularGridInterpolator (linear, bounds_error=False) evaluated on the
+// tensor-product interpolation grid: the host computes, per target x and per
+// target z, the source interval l with g[l] <= v < g[l+1] (last interval at
+// the right end point), the normalised distance and the out-of-bounds flag;
+// the kernel forms the bilinear sum in scipy's term order
+//   v[i,j](1-y0)(1-y1) + v[i,j+1](1-y0)y1 + v[i+1,j]y0(1-y1) + v[i+1,j+1]y0 y1
+// and writes the five fields interleaved into one ring slot (FP64 and/or
+// FP32 copy).  Out-of-bounds targets take the fill value (0, or the mean of
+// vx_x for vx_x).
+#include "dfcsr_common.cuh"
+
+namespace dfcsr {
+
+__global__ void regrid5(const double *__restrict__ f0, const double *__restrict__ f1,
+                        const double *__restrict__ f2, const double *__restrict__ f3,
+                        const double *__restrict__ f4, int snz,
+                        const int32_t *__restrict__ ix, const double *__restrict__ wx,
+                        const uint8_t *__restrict__ oobx, int nxi,
+                        const int32_t *__restrict__ iz, const double *__restrict__ wz,
+                        const uint8_t *__restrict__ oobz, int nzi,
+                        const double *__restrict__ fill4, double *__restrict__ out64,
+                        float *__restrict__ out32) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nxi * nzi) return;
+    const int a = (int)(t / nzi), c = (int)(t % nzi);
+    double v[5];
+    if (oobx[a] || oobz[c]) {
+        v[0] = v[1] = v[2] = v[3] = 0.0;
+        v[4] = *fill4;
+    } else {
+        const int i = ix[a], j = iz[c];
+        const double y0 = wx[a], y1 = wz[c];
+        const double u0 = 1.0 - y0, u1 = 1.0 - y1;
+        const size_t k00 = (size_t)i * snz + j, k01 = k00 + 1, k10 = k00 + snz, k11 = k10 + 1;
+        const double *F[5] = {f0, f1, f2, f3, f4};
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            const double *p = F[q];
+            double r = 0.0;
+            r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k00], u0), u1));
+            r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k01], u0), y1));
+            r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k10], y0), u1));
+            r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k11], y0), y1));
+            v[q] = r;
+        }
+    }
+    if (out64) {
+        double *o = out64 + (size_t)t * 5;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) o[q] = v[q];
+    }
+    if (out32) {
+        float4 *o = reinterpret_cast<float4 *>(out32 + (size_t)t * 8);
+        o[0] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+        o[1] = make_float4((float)v[4], 0.f, 0.f, 0.f);
+    }
+}
+
+}  // namespace dfcsr
+
+using namespace dfcsr;
+
+extern "C" int dfcsr_history_regrid(const double *density, const double *density_x,
+                                    const double *density_z, const double *vx, const double *vx_x,
+                                    int snx, int snz, const int32_t *ix, const double *wx,
+                                    const uint8_t *oobx, int nxi, const int32_t *iz,
+                                    const double *wz, const uint8_t *oobz, int nzi,
+                                    const double *vx_x_fill, double *ring64_slot,
+                                    float *ring32_slot, void *stream) {
+    clear_error();
+    DFCSR_CHECK_ARG(density && density_x && density_z && vx && vx_x && vx_x_fill,
+                    "dfcsr_history_regrid: null field pointer");
+    DFCSR_CHECK_ARG(ix && wx && oobx && iz && wz && oobz, "dfcsr_history_regrid: null index table");
+    DFCSR_CHECK_ARG(snx >= 2 && snz >= 2, "dfcsr_history_regrid: source grid %d x %d too small", snx, snz);
+    DFCSR_CHECK_ARG(nxi >= 1 && nzi >= 1, "dfcsr_history_regrid: empty target grid");
+    DFCSR_CHECK_ARG(ring64_slot || ring32_slot, "dfcsr_history_regrid: no output ring");
+    DFCSR_CHECK_ARG(!ring32_slot || ((uintptr_t)ring32_slot % 16) == 0,
+                    "dfcsr_history_regrid: ring32 slot must be 16-byte aligned");
+    const int64_t cells = (int64_t)nxi * nzi;
+    regrid5<<<(unsigned)((cells + 255) / 256), 256, 0, as_stream(stream)>>>(
+        density, density_x, density_z, vx, vx_x, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,
+        vx_x_fill, ring64_slot, ring32_slot);
+    DFCSR_LAUNCH_CHECK();
+    return DFCSR_OK;
+}

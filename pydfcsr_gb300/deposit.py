@@ -1,0 +1,424 @@
+"""Deposition, distribution functions and the device history ring.
+
+Drop-in for ``pyDFCSR_2D/deposit.py``: ``histogram_cic_2d`` and ``DF_tracker``
+keep the reference's names, argument meaning and attributes; the arrays live
+on the GPU and every computation runs in the sm_103a library:
+
+* ``histogram_cic_2d`` (deposit.py:43-87) -> sort-by-cell deposit,
+  deterministic, both weight channels from one sort;
+* ``DF_tracker.get_DF`` (deposit.py:145-245) -> device moments, deposit and
+  the fused finalisation (threshold, Savitzky-Golay stencils, trapz
+  normalisation, gradients, vx_x fill);
+* ``append_DF`` / ``pop_left_DF`` / ``append_interpolant`` /
+  ``build_interpolant`` (deposit.py:247-426) -> a device ring of
+  (slot, x, z) grids with the five fields interleaved per cell; no per-step
+  copy of the history (the reference re-stacks it every step).
+
+Host numpy attributes of the reference (``density``, ``data_density_interp``
+...) are still available as lazily copied views for compatibility; hot callers
+use the ``*_device`` tensors and the ring directly.
+"""
+import ctypes
+from collections import deque
+
+import numpy as np
+import torch
+
+from . import _lib
+from .coeffs import gradient_table, rgi_axis, savgol_tables
+from .runtime import (as_device_f64, default_workspace, host_to_device, ptr, require_cuda,
+                      stream_handle)
+
+__all__ = ["histogram_cic_2d", "deposit_cic", "beam_moments", "DF_tracker", "HistoryRing",
+           "FIELDS"]
+
+# field order of the ring and of DF_tracker's device field stack
+FIELDS = ("density", "density_x", "density_z", "vx", "vx_x")
+
+
+def beam_moments(x, z, stream=None, ws=None):
+    """Device moments of (x, z): returns a float64 CUDA tensor of 16 values
+    (see dfcsr_beam_moments in include/dfcsr_gb300.h)."""
+    require_cuda()
+    n = x.numel()
+    ws = ws or default_workspace()
+    out = torch.empty(16, dtype=torch.float64, device=x.device)
+    nb = _lib.query("dfcsr_moments_workspace_bytes", n)
+    buf = ws.get("moments", nb)
+    _lib.call("dfcsr_beam_moments", ptr(x), ptr(z), n, ptr(out), ptr(buf), buf.numel(),
+              stream_handle(stream))
+    return out
+
+
+def deposit_cic(q1, q2, w0, w1, nbins_1, bins_start_1, bins_end_1, nbins_2, bins_start_2,
+                bins_end_2, stream=None, ws=None):
+    """Deterministic CIC deposit of up to two weight channels (device tensors).
+
+    ``w0 = None`` deposits unit weights.  Returns (out0, out1 or None), each a
+    float64 CUDA tensor of shape (nbins_1, nbins_2).
+    """
+    require_cuda()
+    n = q1.numel()
+    ws = ws or default_workspace()
+    nb1, nb2 = int(nbins_1), int(nbins_2)
+    out0 = torch.empty((nb1, nb2), dtype=torch.float64, device=q1.device)
+    out1 = torch.empty((nb1, nb2), dtype=torch.float64, device=q1.device) if w1 is not None else None
+    need = _lib.query("dfcsr_deposit_workspace_bytes", n, nb1, nb2)
+    buf = ws.get("deposit", need)
+    _lib.call("dfcsr_deposit_cic2d", ptr(q1), ptr(q2), ptr(w0), ptr(w1), n, nb1,
+              float(bins_start_1), float(bins_end_1), nb2, float(bins_start_2), float(bins_end_2),
+              ptr(out0), ptr(out1), ptr(buf), buf.numel(), stream_handle(stream))
+    return out0, out1
+
+
+def histogram_cic_2d(q1, q2, w, nbins_1, bins_start_1, bins_end_1, nbins_2, bins_start_2,
+                     bins_end_2):
+    """2D cloud-in-cell histogram of ``q1``, ``q2`` weighted by ``w``.
+
+    Same contract as pyDFCSR_2D/deposit.py:43-87: ``nbins_1`` bins from
+    ``bins_start_1`` to ``bins_end_1`` in the first dimension (spacing
+    (end - start) / nbins), linear (CIC) weights, contributions outside the
+    grid dropped.  numpy inputs give a numpy result; torch inputs give a
+    CUDA tensor.
+    """
+    as_numpy = not isinstance(q1, torch.Tensor)
+    a, b, c = as_device_f64(q1).reshape(-1), as_device_f64(q2).reshape(-1), as_device_f64(w).reshape(-1)
+    if not (a.numel() == b.numel() == c.numel()):
+        raise ValueError("q1, q2 and w must have the same length")
+    out, _ = deposit_cic(a, b, c, None, nbins_1, bins_start_1, bins_end_1, nbins_2, bins_start_2,
+                         bins_end_2)
+    return out.cpu().numpy() if as_numpy else out
+
+
+class HistoryRing:
+    """Device ring of (slot, x, z) grids holding the five DF fields per cell.
+
+    ``ring64`` is float64 [cap, nx, nz, 5] (plain FP64 wake); ``ring32`` is
+    float32 [cap, nx, nz, 8] with fields 0..4 used (mixed-precision wake;
+    32-byte cells so a corner's fields load as two aligned float4).  Logical
+    slice k (0 = oldest) lives in physical slot (head + k) % cap.
+    """
+
+    def __init__(self, nx, nz, store64=True, store32=False, cap=8, device=None):
+        self.nx, self.nz = int(nx), int(nz)
+        self.store64, self.store32 = store64, store32
+        self.device = device or torch.device("cuda", torch.cuda.current_device())
+        self.cap = 0
+        self.head = 0
+        self.count = 0
+        self.ring64 = self.ring32 = None
+        self._grow(max(int(cap), 2))
+
+    def _alloc(self, cap):
+        r64 = torch.empty((cap, self.nx, self.nz, 5), dtype=torch.float64,
+                          device=self.device) if self.store64 else None
+        r32 = torch.zeros((cap, self.nx, self.nz, 8), dtype=torch.float32,
+                          device=self.device) if self.store32 else None
+        return r64, r32
+
+    def _grow(self, cap):
+        r64, r32 = self._alloc(cap)
+        for k in range(self.count):
+            src = (self.head + k) % self.cap
+            if r64 is not None:
+                r64[k].copy_(self.ring64[src])
+            if r32 is not None:
+                r32[k].copy_(self.ring32[src])
+        self.ring64, self.ring32 = r64, r32
+        self.cap, self.head = cap, 0
+
+    def nbytes(self):
+        return sum(t.numel() * t.element_size() for t in (self.ring64, self.ring32) if t is not None)
+
+    def push(self):
+        """Reserve the next slot; returns (slot64 view or None, slot32 view or None)."""
+        if self.count == self.cap:
+            self._grow(2 * self.cap)
+        slot = (self.head + self.count) % self.cap
+        self.count += 1
+        return (self.ring64[slot] if self.ring64 is not None else None,
+                self.ring32[slot] if self.ring32 is not None else None)
+
+    def pop_left(self):
+        if self.count == 0:
+            raise IndexError("pop from an empty history ring")
+        self.head = (self.head + 1) % self.cap
+        self.count -= 1
+
+    def clear(self, nx=None, nz=None):
+        if (nx is not None and int(nx) != self.nx) or (nz is not None and int(nz) != self.nz):
+            self.nx, self.nz = int(nx), int(nz)
+            self.ring64, self.ring32 = self._alloc(self.cap)
+        self.head = 0
+        self.count = 0
+
+    def stacked(self, field):
+        """Host copy [count, nx, nz] of one field in time order (compatibility)."""
+        f = FIELDS.index(field)
+        idx = [(self.head + k) % self.cap for k in range(self.count)]
+        if self.ring64 is not None:
+            return self.ring64[idx][..., f].cpu().numpy()
+        return self.ring32[idx][..., f].double().cpu().numpy()
+
+
+class _DFEntry:
+    __slots__ = ("x_grids", "z_grids", "fields", "scalars", "t", "sigma_x", "sigma_z")
+
+    def __init__(self, x_grids, z_grids, fields, scalars, t, sigma_x, sigma_z):
+        self.x_grids, self.z_grids = x_grids, z_grids
+        self.fields, self.scalars = fields, scalars
+        self.t, self.sigma_x, self.sigma_z = t, sigma_x, sigma_z
+
+
+class DF_tracker:
+    """Distribution functions of the beam and their history, on the GPU.
+
+    Mirrors ``pyDFCSR_2D.deposit.DF_tracker`` (deposit.py:90-426).  Extra
+    keyword arguments (not in the reference):
+
+    * ``precision``: ``'fp64'`` keeps the FP64 ring for the plain wake,
+      ``'mixed'`` the FP32 ring for the mixed-precision wake, ``'both'`` both.
+    * ``grid_rule``: ``'reference'`` reproduces get_DF's fallback to a 100x100
+      grid and window 5 when sigma_x / sigma_x(slice) <= 5
+      (deposit.py:157-168); ``'configured'`` always uses the configured bins
+      and window.
+    """
+
+    def __init__(self, input_dic={}, precision="fp64", grid_rule="reference", workspace=None):
+        self.configure_params(**input_dic)
+        if precision not in ("fp64", "mixed", "both"):
+            raise ValueError("precision must be 'fp64', 'mixed' or 'both'")
+        if grid_rule not in ("reference", "configured"):
+            raise ValueError("grid_rule must be 'reference' or 'configured'")
+        self.precision = precision
+        self.grid_rule = grid_rule
+        self.ws = workspace
+        self.sigma_x = self.sigma_z = None
+        self.x_grids = self.z_grids = None
+        self.start_time = 0.0
+        self.t = 0.0
+        self.slope_log = deque([])
+        self.DF_log = deque([])
+        self.sigma_x_log = deque([])
+        self.sigma_z_log = deque([])
+        self.time_log = deque([])
+        self.sigma_x_interp = self.sigma_z_interp = None
+        self.time_interp = deque([])
+        self.interp_start = 0
+        self.end_time = 0.0
+        self.x_grid_interp = self.z_grid_interp = None
+        self.ring = None
+        self._cur = None
+        self.stats = None
+        self.reinterpolated = False
+
+    def configure_params(self, xbins=100, zbins=100, xlim=5, zlim=5, filter_order=0,
+                         filter_window=0, velocity_threhold=5, upper_limit=None):
+        self.xbins = xbins
+        self.zbins = zbins
+        self.xlim = xlim
+        self.zlim = zlim
+        self.velocity_threhold = velocity_threhold
+        self.filter_order = filter_order
+        self.filter_window = filter_window
+        self.upper_limit = upper_limit
+
+    # ------------------------------------------------------------- get_DF
+    def _workspace(self):
+        return self.ws or default_workspace()
+
+    def get_DF(self, x, z, px, t, stream=None):
+        """Deposit and finalise the current DF (deposit.py:145-245)."""
+        require_cuda()
+        xd, zd, pxd = (as_device_f64(a).reshape(-1) for a in (x, z, px))
+        ws = self._workspace()
+        mom = beam_moments(xd, zd, stream, ws)
+        st = mom.cpu().numpy()
+        self.stats = st
+        sigma_x, sigma_z = float(st[3]), float(st[4])
+        self.sigma_x, self.sigma_z = sigma_x, sigma_z
+        self.xmean, self.zmean = float(st[1]), float(st[2])
+        with np.errstate(all="ignore"):
+            frac = np.float64(sigma_x) / np.float64(st[8])
+        if frac > 5 or self.grid_rule == "configured":
+            xb, zb, win = int(self.xbins), int(self.zbins), int(self.filter_window)
+        else:
+            xb, zb, win = 100, 100, 5
+        x0 = self.xmean - self.xlim * sigma_x
+        x1 = self.xmean + self.xlim * sigma_x
+        z0 = self.zmean - self.zlim * sigma_z
+        z1 = self.zmean + self.zlim * sigma_z
+        xg = np.linspace(x0, x1, xb)
+        zg = np.linspace(z0, z1, zb)
+        density, vxsum = deposit_cic(xd, zd, None, pxd, xb, x0, x1, zb, z0, z1, stream, ws)
+        fields = torch.empty((5, xb, zb), dtype=torch.float64, device=xd.device)
+        fields[0].copy_(density)
+        fields[3].copy_(vxsum)
+        sc = torch.zeros(8, dtype=torch.float64, device=xd.device)
+        self._finalize(fields, sc, xg, zg, win, stream, ws)
+        self.x_grids, self.z_grids = xg, zg
+        self._cur = _DFEntry(xg, zg, fields, sc, t, sigma_x, sigma_z)
+        self.t = t
+        self.bins = (xb, zb, win)
+
+    def _finalize(self, fields, sc, xg, zg, win, stream, ws):
+        xb, zb = xg.size, zg.size
+        coeff, lo, hi = savgol_tables(win, int(self.filter_order))
+        gx, gxu, gxdx = gradient_table(xg)
+        gz, gzu, gzdx = gradient_table(zg)
+        # one host->device copy of all per-step constants
+        parts = [coeff, lo.ravel(), hi.ravel(), gx.ravel(), gz.ravel(), np.diff(xg), np.diff(zg)]
+        sizes = [p.size for p in parts]
+        blob = host_to_device(np.concatenate(parts))
+        offs = np.concatenate([[0], np.cumsum(sizes)])
+        base = blob.data_ptr()
+        P = _lib.DFParams()
+        P.nx, P.nz, P.window, P.order = xb, zb, int(win), int(self.filter_order)
+        P.velocity_threshold = float(self.velocity_threhold)
+        (P.sg_coeff, P.sg_lo, P.sg_hi, P.gx, P.gz, P.dxg, P.dzg) = [base + 8 * int(o) for o in offs[:7]]
+        P.gx_uniform, P.gz_uniform = int(gxu), int(gzu)
+        P.gx_dx, P.gz_dx = gxdx, gzdx
+        need = _lib.query("dfcsr_df_workspace_bytes", xb, zb)
+        buf = ws.get("df", need)
+        _lib.call("dfcsr_df_finalize", ctypes.byref(P), ptr(fields[0]), ptr(fields[3]),
+                  ptr(fields[1]), ptr(fields[2]), ptr(fields[4]), ptr(sc), ptr(buf), buf.numel(),
+                  stream_handle(stream))
+        self._blob = blob   # keep the constants alive until the stream consumes them
+
+    # compatibility views of the current DF (host copies)
+    def _field(self, name):
+        return None if self._cur is None else self._cur.fields[FIELDS.index(name)].cpu().numpy()
+
+    density = property(lambda self: self._field("density"))
+    density_x = property(lambda self: self._field("density_x"))
+    density_z = property(lambda self: self._field("density_z"))
+    vx = property(lambda self: self._field("vx"))
+    vx_x = property(lambda self: self._field("vx_x"))
+
+    @property
+    def fields_device(self):
+        """Current DF as a float64 CUDA tensor [5, nx, nz] in FIELDS order."""
+        return None if self._cur is None else self._cur.fields
+
+    # ----------------------------------------------------------- history
+    def append_DF(self):
+        """append current DF to the log (deposit.py:247-256)"""
+        self.DF_log.append(self._cur)
+        self.time_log.append(self.t)
+        self.sigma_x_log.append(self.sigma_x)
+        self.sigma_z_log.append(self.sigma_z)
+        self.end_time = self.t
+
+    def pop_left_DF(self, new_start_time):
+        """pop history until new_start_time (deposit.py:258-280)"""
+        while self.start_time < new_start_time:
+            self.DF_log.popleft()
+            self.time_log.popleft()
+            self.sigma_x_log.popleft()
+            self.sigma_z_log.popleft()
+            self.start_time = self.time_log[0]
+        while self.interp_start < new_start_time:
+            self.ring.pop_left()
+            self.time_interp.popleft()
+            self.interp_start = self.time_interp[0]
+
+    def pop_right_DF(self):
+        """pop the newest DF from the log (deposit.py:283-292)"""
+        self.DF_log.pop()
+        self.time_log.pop()
+        self.sigma_x_log.pop()
+        self.sigma_z_log.pop()
+        self.end_time = self.time_log[-1]
+
+    def _regrid_into_ring(self, entry, stream=None):
+        ix, wx, ox = rgi_axis(entry.x_grids, self.x_grid_interp)
+        iz, wz, oz = rgi_axis(entry.z_grids, self.z_grid_interp)
+        nxi, nzi = ix.size, iz.size
+        # pack the index tables into one copy: int32 idx | f64 w | u8 oob
+        blob = np.zeros(8 * (2 * nxi + 2 * nzi) + 2 * (nxi + nzi) + 64, dtype=np.uint8)
+        o = 0
+        views = []
+        for arr in (wx, wz, ix, iz, ox, oz):
+            b = np.ascontiguousarray(arr).view(np.uint8)
+            blob[o:o + b.size] = b
+            views.append(o)
+            o += (b.size + 15) // 16 * 16
+        dev = host_to_device(blob[:o + 16])
+        base = dev.data_ptr()
+        s64, s32 = self.ring.push()
+        f = entry.fields
+        _lib.call("dfcsr_history_regrid", ptr(f[0]), ptr(f[1]), ptr(f[2]), ptr(f[3]), ptr(f[4]),
+                  f.shape[1], f.shape[2],
+                  ctypes.c_void_p(base + views[2]), ctypes.c_void_p(base + views[0]),
+                  ctypes.c_void_p(base + views[4]), nxi,
+                  ctypes.c_void_p(base + views[3]), ctypes.c_void_p(base + views[1]),
+                  ctypes.c_void_p(base + views[5]), nzi,
+                  ctypes.c_void_p(entry.scalars.data_ptr() + 8 * 4),
+                  ptr(s64), ptr(s32), stream_handle(stream))
+        self._regrid_blob = dev
+
+    def _new_ring(self, nxi, nzi):
+        store64 = self.precision in ("fp64", "both")
+        store32 = self.precision in ("mixed", "both")
+        if self.ring is None:
+            self.ring = HistoryRing(nxi, nzi, store64, store32, cap=max(8, len(self.DF_log) + 4))
+        else:
+            self.ring.clear(nxi, nzi)
+
+    def append_interpolant(self, formation_length, n_formation_length, stream=None):
+        """Trim the window and append the current DF to the interpolant
+        (deposit.py:312-392)."""
+        start_point = np.amax((0, self.end_time - n_formation_length * formation_length))
+        self.pop_left_DF(new_start_time=start_point)
+        if self.sigma_x_interp and self.sigma_z_interp and \
+                2 > self.sigma_x / self.sigma_x_interp > 1 / 2 and \
+                2 > self.sigma_z / self.sigma_z_interp > 1 / 2:
+            self.time_interp.append(self.t)
+            self._regrid_into_ring(self._cur, stream)
+            self.reinterpolated = False
+            return
+        max_sigma_x, min_sigma_x = np.max(self.sigma_x_log), np.min(self.sigma_x_log)
+        max_sigma_z, min_sigma_z = np.max(self.sigma_z_log), np.min(self.sigma_z_log)
+        xbins = int(500 * (max_sigma_x / min_sigma_x))
+        zbins = int(500 * (max_sigma_z / min_sigma_z))
+        if isinstance(self.upper_limit, int):
+            xbins = min(xbins, self.upper_limit)
+            zbins = min(zbins, self.upper_limit)
+        self.sigma_x_interp = max_sigma_x
+        self.sigma_z_interp = max_sigma_z
+        self.x_grid_interp = np.linspace(self.xmean - 5 * self.sigma_x_interp,
+                                         self.xmean + 5 * self.sigma_x_interp, xbins)
+        self.z_grid_interp = np.linspace(self.zmean - 5 * self.sigma_z_interp,
+                                         self.zmean + 5 * self.sigma_z_interp, zbins)
+        self._new_ring(xbins, zbins)
+        self.time_interp = self.time_log.copy()
+        for entry in self.DF_log:
+            self._regrid_into_ring(entry, stream)
+        self.reinterpolated = True
+
+    def build_interpolant(self):
+        """Interpolant parameters over the ring (deposit.py:395-426); the
+        history itself is not copied."""
+        self.min_x, self.max_x = self.time_interp[0], self.time_interp[-1]
+        self.min_y, self.max_y = self.x_grid_interp[0], self.x_grid_interp[-1]
+        self.min_z, self.max_z = self.z_grid_interp[0], self.z_grid_interp[-1]
+        self.delta_x = (self.max_x - self.min_x) / (len(self.time_interp) - 1)
+        self.delta_y = (self.max_y - self.min_y) / (self.x_grid_interp.shape[0] - 1)
+        self.delta_z = (self.max_z - self.min_z) / (self.z_grid_interp.shape[0] - 1)
+
+    # stacked host copies, like the reference's data_*_interp arrays
+    data_density_interp = property(lambda self: self.ring.stacked("density"))
+    data_density_x_interp = property(lambda self: self.ring.stacked("density_x"))
+    data_density_z_interp = property(lambda self: self.ring.stacked("density_z"))
+    data_vx_interp = property(lambda self: self.ring.stacked("vx"))
+    data_vx_x_interp = property(lambda self: self.ring.stacked("vx_x"))
+
+    def job_fields(self):
+        """Ring pointers and interpolant parameters for a dfcsr_wake_job."""
+        r = self.ring
+        return dict(ring64=r.ring64.data_ptr() if r.ring64 is not None else None,
+                    ring32=r.ring32.data_ptr() if r.ring32 is not None else None,
+                    cap=r.cap, head=r.head, nt=r.count, nx=r.nx, nz=r.nz,
+                    t_min=float(self.min_x), x_min=float(self.min_y), z_min=float(self.min_z),
+                    t_delta=float(self.delta_x), x_delta=float(self.delta_y),
+                    z_delta=float(self.delta_z))

@@ -1,0 +1,70 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every symbol the
+header declares (no GPU needed: nothing here launches a kernel)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from pydfcsr_gb300 import _lib, build
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "dfcsr_gb300.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(dfcsr_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_builds_and_loads():
+    path = build.build()
+    assert os.path.exists(path)
+    lib = _lib.load()
+    assert lib.dfcsr_version() >= 100
+
+
+def test_every_header_symbol_exported():
+    lib = ctypes.CDLL(build.build())
+    names = header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in the header but not exported"
+    # the binding covers every declared entry point
+    assert set(names) <= set(_lib.EXPORTS), set(names) - set(_lib.EXPORTS)
+
+
+def test_struct_layouts_match():
+    lib = _lib.load()
+    assert lib.dfcsr_abi_sizeof(0) == ctypes.sizeof(_lib.DFParams)
+    assert lib.dfcsr_abi_sizeof(1) == ctypes.sizeof(_lib.WakeJob)
+    assert lib.dfcsr_abi_sizeof(7) == 0
+
+
+def test_status_names_and_sizes():
+    lib = _lib.load()
+    assert lib.dfcsr_status_name(0) == b"OK"
+    assert lib.dfcsr_status_name(6) == b"ADMISSION_REFUSED"
+    assert lib.dfcsr_deposit_workspace_bytes(1000, 64, 64) > 4 * 1000
+    assert lib.dfcsr_deposit_workspace_bytes(-1, 64, 64) == 0
+    assert lib.dfcsr_df_workspace_bytes(64, 64) >= 6 * 64 * 64 * 8
+    assert lib.dfcsr_wake_workspace_bytes(100, 100, 4096) > 0
+
+
+def test_bad_arguments_fail_without_gpu():
+    """Argument checks run before any device work, so they are testable here."""
+    with pytest.raises(_lib.DfcsrBadArgument):
+        _lib.call("dfcsr_deposit_cic2d", None, None, None, None, 10, 0, 0.0, 1.0, 4, 0.0, 1.0,
+                  None, None, None, 0, None)
+    with pytest.raises(_lib.DfcsrBadArgument, match="window_length"):
+        p = _lib.DFParams()
+        p.nx, p.nz, p.window, p.order = 8, 8, 4, 2
+        dummy = ctypes.c_void_p(16)
+        _lib.call("dfcsr_df_finalize", ctypes.byref(p), dummy, dummy, dummy, dummy, dummy, dummy,
+                  None, 0, None)
+    with pytest.raises(_lib.DfcsrBadArgument):
+        _lib.call("dfcsr_wake_mixed", ctypes.c_void_p(16), None, ctypes.c_void_p(16),
+                  ctypes.c_void_p(16), 5, 2000, 100, 0, ctypes.c_void_p(16), ctypes.c_void_p(16),
+                  None, 0, None)
+    assert "xbins" in _lib.load().dfcsr_last_error().decode()
