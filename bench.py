@@ -1,0 +1,456 @@
+#!/usr/bin/env python
+"""Wake-point throughput of the per-step CSR wake path on one GB300.
+
+Workload (the metric's configuration): the four-dipole chicane with a
+2e6-particle Gaussian beam (sigma_z 50 um, sigma_x 20 um, chirp h = -10 1/m,
+sigma_delta 1e-4, 1 GeV, seeded), 256x256 deposit grid (SG window 9, order 2),
+64x64 observation mesh every step, 100 steps over 6.5 m, integration bins
+100x100, n_formation_length 1.5, mixed precision (FP32 bulk, FP64 retarded
+geometry).  Synthetic data (seeded numpy beam, r_gen6 transport between
+steps).
+
+One step = get_DF (device moments, deposit, DF finalisation) + append_DF +
+append_interpolant (history ring regrid) + build_interpolant +
+get_CSR_mesh + the wake on all 4096 mesh points.
+
+  value        wake points/s with each step's particles already in HBM
+  e2e          the same through the public CSR2D calls with HOST buffers:
+               pinned-host -> device copy of (x, px, z) every step and the
+               (dE_dct, x_kick) result read back every step
+  roofline     dominant kernel (wake_mixed_integral), CUDA events on its
+               launch stream inside the timed region
+  cpu_baseline the CPU oracle (C restatement of the reference, all threads)
+               on a bounded sample of the same workload
+
+``--impl reference`` times the CPU oracle (the reference's algorithm restated
+in C + numpy; the reference itself is Python/numba and not available on the
+GPU host) on the same config and prints the same metric.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "chicane_c2"
+METRIC = "wake points/sec (64x64 mesh per step, chicane 2e6 particles, 256x256 grid)"
+UNIT = "wake_points/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--particles", type=int, default=None, help="override N (testing only)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison leg")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def lattice_for(wl, total_steps):
+    """The workload's chicane, extended by a drift if more steps are asked."""
+    from pydfcsr_gb300.synthetic import StepPlan
+    lat = wl.lattice.copy()
+    plan = StepPlan(lat)
+    if total_steps + 1 > len(plan.positions):
+        extra = (total_steps + 1 - len(plan.positions) + 1) * float(lat["step_size"])
+        lat["Dtail"] = {"type": "drift", "L": extra, "nsep": 1}
+    return lat
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# -------------------------------------------------------------- GPU arm
+def make_run(wl, lattice, precision, seed_offset=0):
+    from pydfcsr_gb300.harness import WakeRun
+    beam = wl.beam(seed=(2 + seed_offset))
+    return WakeRun(lattice, beam, wl.deposit, wl.integration, wl.mesh, precision=precision,
+                   grid_rule="configured", host_transport=False), beam
+
+
+def device_step_sets(run, steps):
+    """Transport on the device once (before timing) and keep every step's
+    particle set resident: list of (6, N) float64 CUDA tensors."""
+    import torch
+    sets = []
+    cur = run.beam.particle.clone()
+    for k in range(1, steps + 1):
+        R = torch.as_tensor(run.plan.matrix(k), device=cur.device)
+        cur = (R @ cur).contiguous()
+        sets.append(cur)
+    return sets
+
+
+def timed_steps(run, sets, first, count, precision, events=None, wake=True):
+    """Run steps first..first+count-1 from device-resident particle sets;
+    ``events`` (list) receives one (start, end) CUDA event pair per step."""
+    import torch
+    csr = run.csr
+    stream = torch.cuda.current_stream()
+    for k in range(first, first + count):
+        if events is not None:
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[0].record(stream)
+        run.beam.particle = sets[k - 1]
+        run.beam.update_status()
+        run.beam.position = float(run.plan.positions[k])
+        run.beam.step = k
+        lf = run.plan.formation_length(k, run.beam.sigma_z)
+        csr.update_history(lf)
+        if wake:
+            csr.get_CSR_mesh()
+            s = torch.from_numpy(run.beam.position + csr.CSR_zmesh).cuda()
+            x = torch.from_numpy(csr.CSR_xmesh).cuda()
+            run.last = csr.wake_device(s, x, precision)
+        if events is not None:
+            ev[1].record(stream)
+            events.append(ev)
+
+
+def e2e_steps(run, host_sets, first, count, precision, dev_buf):
+    """Steps through the public API with host buffers: H2D of (x, px, z)
+    from pinned memory, CSR2D calls, D2H of (dE_dct, x_kick)."""
+    csr = run.csr
+    h2d = d2h = 0
+    for k in range(first, first + count):
+        xpz = host_sets[k - 1]                      # pinned (3, N): x, px, z
+        dev_buf[0].copy_(xpz[0], non_blocking=True)
+        dev_buf[1].copy_(xpz[1], non_blocking=True)
+        dev_buf[4].copy_(xpz[2], non_blocking=True)
+        h2d += xpz.numel() * 8
+        run.beam.particle = dev_buf
+        run.beam.update_status()
+        run.beam.position = float(run.plan.positions[k])
+        lf = run.plan.formation_length(k, run.beam.sigma_z)
+        csr.update_history(lf)
+        csr.get_CSR_mesh()
+        csr.calculate_2D_CSR(precision)             # reads dE_dct, x_kick back to the host
+        d2h += csr.dE_dct.nbytes + csr.x_kick.nbytes
+    return h2d // count, d2h // count
+
+
+def gpu_arm(a):
+    import torch
+    import torch.distributed as dist
+    from pydfcsr_gb300 import _lib
+    from pydfcsr_gb300.synthetic import workload
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    wl = workload(WORKLOAD, n_particles=a.particles)
+    W, K = max(a.warmup, 0), a.steps
+    lattice = lattice_for(wl, W + K)
+    run, beam0 = make_run(wl, lattice, a.precision, seed_offset=rank)
+    sets = device_step_sets(run, W + K)
+    npts = wl.mesh["xbins"] * wl.mesh["zbins"]
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up (builds the history; untimed)
+    timed_steps(run, sets, 1, W, a.precision)
+    barrier()
+    _lib.timing_reset()
+    _lib.timing_enable(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    t0 = time.perf_counter()
+    step_events = []
+    e0.record(stream)
+    timed_steps(run, sets, W + 1, K, a.precision, events=step_events)
+    e1.record(stream)
+    barrier()
+    wall = time.perf_counter() - t0
+    ck = clocks.stop()
+    _lib.timing_enable(False)
+    dev_ms = e0.elapsed_time(e1)
+    kname = "wake_mixed_integral" if a.precision == "mixed" else "wake_fp64"
+    k_ms, k_n = _lib.timing_read(kname)
+    launches = {n: _lib.timing_read(n)[1] for n in
+                ("beam_moments", "deposit_cic2d", "df_finalize", "history_regrid", "wake_fp64",
+                 "wake_mixed_geometry", "wake_mixed_integral", "wake_mixed_band")}
+    step_ms = dev_ms / K
+    if world > 1:
+        t = torch.tensor([step_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = world * npts * 1000.0 / step_ms
+
+    lat = np.array([ev[0].elapsed_time(ev[1]) for ev in step_events])
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+           "warmup": W, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64" if a.precision == "mixed" else "f64",
+           "data": "synthetic (seeded numpy Gaussian beam, r_gen6 transport)",
+           "config": {"workload": "chicane_c2: 4 dipoles 0.5 m +-0.05 rad, drifts 2/0.5/2 m, "
+                                  "1 GeV, N=%d, sigma_z 50um, sigma_x 20um, h=-10/m, grid 256x256, "
+                                  "SG 9/2, mesh 64x64 every step, 100x100 integration bins"
+                                  % run.beam.n_particle,
+                      "precision": a.precision, "l2": "inputs larger than L2: distinct 96 MB "
+                      "particle set per step; history ring >= 190 MB"},
+           "wall_s_timed": wall, "clocks": ck,
+           "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "definition": "device time of one full step (DF + history + wake)"}}
+
+    # roofline of the dominant kernel
+    from pydfcsr_gb300.synthetic import StepPlan  # noqa: F401
+    ip = wl.integration
+    pts_per_obs = None
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    # integrand points per launch: every region of every observation point
+    # (3 regions x 100x100 + 2*100*100 unchirped, 4 regions chirped)
+    slope = abs(run.beam._slope[0])
+    per_obs = (5 if slope > 1 else 4) * ip["xbins"] * ip["zbins"]
+    if k_n:
+        launch_ms = k_ms / k_n
+        # launches per step: batches of observation points
+        per_launch_pts = npts * per_obs * K / k_n
+        bytes_per_pt = 160 if a.precision == "mixed" else 320
+        achieved = per_launch_pts * bytes_per_pt / (launch_ms * 1e-3) / 1e9
+        out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                           "frac": achieved / hbm, "traffic": None,
+                           "kernel": kname, "launch_ms": launch_ms, "launches": k_n,
+                           "algorithmic": f"{bytes_per_pt} B gathered per integrand point "
+                                          f"(5 fields x 8 corners), {per_launch_pts:.3g} points per "
+                                          "launch; gathers are served mostly from L1/L2",
+                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+    out["gpu_launches"] = int(sum(launches.values()))
+    out["kernel_launches_by_name"] = launches
+
+    # plain FP64 leg on the same steps (for the mixed vs FP64 speed-up)
+    if not a.no_fp64 and a.precision == "mixed":
+        r64, _ = make_run(wl, lattice, "fp64", seed_offset=rank)
+        K64 = min(K, 3)
+        timed_steps(r64, sets, 1, W + K - K64 - 1, "fp64", wake=False)
+        timed_steps(r64, sets, W + K - K64, 1, "fp64")          # warm the FP64 kernel
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        timed_steps(r64, sets, W + K - K64 + 1, K64, "fp64")
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = f0.elapsed_time(f1) / K64
+        # accuracy of the mixed result vs the FP64 kernel on the last step
+        dE32, xk32 = (t.cpu().numpy() for t in run.last)       # step W + K, mixed
+        dE64, xk64 = (t.cpu().numpy() for t in r64.last)       # step W + K, plain FP64
+
+        def rel(a_, b_):
+            p = np.max(np.abs(b_))
+            return float(np.max(np.abs(a_ - b_) / np.maximum(np.abs(b_), 1e-3 * p)))
+
+        out["plain_fp64"] = {"ms_per_step": ms64, "value": npts * 1000.0 / ms64, "steps": K64,
+                             "mixed_speedup": ms64 / step_ms,
+                             "mixed_vs_fp64_max_rel_err": {"dE": rel(dE32, dE64),
+                                                           "xkick": rel(xk32, xk64)},
+                             "error_definition": "max |a-b| / max(|b|, 1e-3 max|b|) over the "
+                                                 "64x64 mesh of the last timed step"}
+        del r64
+
+    # end to end through the public API with host buffers
+    if not a.no_e2e:
+        re2e, _ = make_run(wl, lattice, a.precision, seed_offset=rank)
+        host_sets = []
+        for t in sets[:W + K]:
+            h = torch.empty((3, t.shape[1]), dtype=torch.float64, pin_memory=True)
+            h.copy_(t[[0, 1, 4]])
+            host_sets.append(h)
+        dev_buf = torch.zeros_like(sets[0])
+        e2e_steps(re2e, host_sets, 1, W, a.precision, dev_buf)
+        barrier()
+        g0 = time.perf_counter()
+        h2d, d2h = e2e_steps(re2e, host_sets, W + 1, K, a.precision, dev_buf)
+        barrier()
+        e2e_s = time.perf_counter() - g0
+        out["e2e"] = {"value": world * npts * K / e2e_s, "unit": UNIT,
+                      "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                      "ms_per_step": e2e_s * 1000 / K}
+        del re2e, host_sets
+
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(wl, lattice, sample_steps=2, warm_steps=4, n_obs=32)
+    if world > 1:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+
+
+# ------------------------------------------------------------- CPU oracle
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_oracle_steps(wl, lattice, warm_steps, sample_steps, n_obs, threads):
+    """Oracle over steps 1..warm+sample; returns per-step seconds for the
+    DF/history part and the wake extrapolated to the full mesh."""
+    from oracle import oracle as O
+    from pydfcsr_gb300.synthetic import StepPlan
+    plan = StepPlan(lattice)
+    coords = wl.beam()
+    tr = O.DFTracker(wl.deposit, grid_rule="configured")
+    tr.get_DF(coords[0], coords[4], coords[1], 0.0)
+    tr.append_DF()
+    tr.append_interpolant(float("inf"), wl.integration["n_formation_length"])
+    s, rho, dist_, nsep, tab, nv, tau = O.reference_trajectory(lattice, 2000)
+    npts = wl.mesh["xbins"] * wl.mesh["zbins"]
+    per_step = []
+    for k in range(1, warm_steps + sample_steps + 1):
+        t0 = time.perf_counter()
+        coords = plan.matrix(k) @ coords
+        pos = plan.positions[k]
+        st = O.beam_stats(coords[0], coords[4])
+        lf = plan.formation_length(k, st["sigma_z"])
+        tr.get_DF(coords[0], coords[4], coords[1], pos)
+        tr.append_DF()
+        tr.append_interpolant(lf, wl.integration["n_formation_length"])
+        tr.build_interpolant()
+        t_df = time.perf_counter() - t0
+        if k <= warm_steps:
+            continue
+        xm, zm, _, _ = O.csr_mesh(st, wl.mesh["xbins"], wl.mesh["zbins"], wl.mesh["xlim"],
+                                  wl.mesh["zlim"])
+        w = O.WakeOracle(tr, (s, rho, dist_, tab, nv, tau), pos, st["sigma_z"], st["sigma_x"],
+                         st["slope"][0], st["mean_x"], lf, wl.integration["n_formation_length"],
+                         wl.integration["zbins"], wl.integration["xbins"])
+        idx = np.linspace(0, npts - 1, n_obs).astype(int)
+        t1 = time.perf_counter()
+        w.points(pos + zm[idx], xm[idx], nthreads=threads)
+        t_w = (time.perf_counter() - t1) * npts / n_obs
+        per_step.append(t_df + t_w)
+    return float(np.mean(per_step)), npts
+
+
+def cpu_baseline(wl, lattice, sample_steps, warm_steps, n_obs):
+    threads = cpu_threads()
+    sec, npts = cpu_oracle_steps(wl, lattice, warm_steps, sample_steps, n_obs, threads)
+    return {"value": npts / sec, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"CPU oracle (C restatement of get_CSR_wake/get_CSR_integrand, numpy "
+                      f"DF/history) on the same chicane beam: steps 1..{warm_steps + sample_steps} "
+                      f"built in full, wake on {n_obs} of {npts} mesh points at each of the last "
+                      f"{sample_steps} steps, scaled to the full mesh; {threads} threads"}
+
+
+def reference_arm(a):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from pydfcsr_gb300.synthetic import workload
+    wl = workload(WORKLOAD, n_particles=a.particles)
+    W, K = max(a.warmup, 0), a.steps
+    lattice = lattice_for(wl, W + K)
+    threads = cpu_threads()
+    # each timed step: the full DF/history step plus the wake on a sample of
+    # the mesh (scaled); warm-up steps build the history (untimed)
+    n_obs = 16
+    sec, npts = cpu_oracle_steps(wl, lattice, warm_steps=min(W, 4), sample_steps=min(K, 3),
+                                 n_obs=n_obs, threads=threads)
+    value = npts / sec
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": min(K, 3),
+           "warmup": min(W, 4), "ms_per_step": sec * 1000, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded numpy Gaussian beam, r_gen6 transport)",
+           "config": {"workload": WORKLOAD, "precision": "fp64 (reference algorithm)"},
+           "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": f"wake on {n_obs} of {npts} mesh points per step, scaled; "
+                                      "DF/history steps in full"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        reference_arm(a)
+    else:
+        gpu_arm(a)
+
+
+if __name__ == "__main__":
+    main()

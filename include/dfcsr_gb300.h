@@ -45,6 +45,17 @@ const char *dfcsr_status_name(int status);
  * bindings that lay the structs out themselves); 0 for other values. */
 size_t dfcsr_abi_sizeof(int which);
 
+/* Optional kernel timing (off by default).  When enabled, the entry points
+ * record CUDA events around their main kernels on the launch stream;
+ * dfcsr_timing_collect() waits for the recorded events and adds their
+ * durations to per-kernel totals, read with dfcsr_timing_get(name, ...).
+ * Names: beam_moments, deposit_cic2d, df_finalize, history_regrid,
+ * wake_fp64, wake_mixed_geometry, wake_mixed_integral, wake_mixed_band. */
+void dfcsr_timing_enable(int on);
+int dfcsr_timing_collect(void);
+int dfcsr_timing_get(const char *name, double *total_ms, long long *launches);
+void dfcsr_timing_reset(void);
+
 /* ------------------------------------------------------------------------
  * Beam moments.  Replaces the numpy statistics used by DF_tracker.get_DF
  * (deposit.py:147-159: std/mean of x and z, slice std of x where
@@ -65,7 +76,8 @@ int dfcsr_beam_moments(const double *x, const double *z, int64_t n, double *out,
  * called twice per step by get_DF (deposit.py:172-182) with w = 1 and
  * w = px.  Both weight channels are deposited from one sort:
  *   out0 = CIC(q1, q2, w0 or 1 if w0 == NULL)   [nb1][nb2] row-major
- *   out1 = CIC(q1, q2, w1)                       (skipped if w1 == NULL)
+ *   out1 = CIC(q1, q2, w1)                       (skipped if out1 == NULL;
+ *                                                 w1 required when n > 0)
  * Bin spacing (end - start) / nbins, lower bin floor(cell), weights
  * 1 - frac, bounds-checked corners - exactly the reference's rule.
  * Deterministic: particles are sorted by lower cell (stable LSD radix sort)

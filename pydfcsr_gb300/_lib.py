@@ -98,6 +98,11 @@ _SIGS = [
     ("dfcsr_last_error", ctypes.c_char_p, []),
     ("dfcsr_status_name", ctypes.c_char_p, [_c_int]),
     ("dfcsr_abi_sizeof", _c_size, [_c_int]),
+    ("dfcsr_timing_enable", None, [_c_int]),
+    ("dfcsr_timing_collect", _c_int, []),
+    ("dfcsr_timing_get", _c_int, [ctypes.c_char_p, ctypes.POINTER(_c_double),
+                                  ctypes.POINTER(ctypes.c_longlong)]),
+    ("dfcsr_timing_reset", None, []),
     ("dfcsr_moments_workspace_bytes", _c_size, [_c_i64]),
     ("dfcsr_beam_moments", _c_int, [_p, _p, _c_i64, _p, _p, _c_size, _p]),
     ("dfcsr_deposit_workspace_bytes", _c_size, [_c_i64, _c_int, _c_int]),
@@ -167,3 +172,20 @@ def call(name, *args):
 def query(name, *args):
     """Call a size / info function (no status)."""
     return getattr(load(), name)(*args)
+
+
+def timing_enable(on=True):
+    load().dfcsr_timing_enable(1 if on else 0)
+
+
+def timing_reset():
+    load().dfcsr_timing_reset()
+
+
+def timing_read(name):
+    """(total_ms, launches) of a kernel since the last reset (collects first)."""
+    lib = load()
+    lib.dfcsr_timing_collect()
+    ms, n = ctypes.c_double(), ctypes.c_longlong()
+    lib.dfcsr_timing_get(name.encode(), ctypes.byref(ms), ctypes.byref(n))
+    return ms.value, n.value

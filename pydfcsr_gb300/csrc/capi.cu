@@ -51,3 +51,89 @@ extern "C" size_t dfcsr_abi_sizeof(int which) {
         default: return 0;
     }
 }
+
+// --------------------------------------------------------------- timing
+// Optional per-kernel timing: when enabled, entry points bracket their main
+// kernels with CUDA events recorded on the launch stream.  Events are read
+// (and the totals folded) only by dfcsr_timing_collect, after the timed
+// region, so enabling this adds two event records per kernel and no sync.
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace dfcsr {
+
+struct PendingTiming {
+    std::string name;
+    cudaEvent_t a, b;
+};
+
+static std::mutex g_tmu;
+static bool g_timing = false;
+static std::vector<PendingTiming> g_pending;
+static std::map<std::string, std::pair<double, long long>> g_totals;
+
+bool timing_on() { return g_timing; }
+
+void timing_begin(const char *name, cudaStream_t s, void **token) {
+    *token = nullptr;
+    if (!g_timing) return;
+    PendingTiming *p = new PendingTiming{name, nullptr, nullptr};
+    if (cudaEventCreate(&p->a) != cudaSuccess || cudaEventCreate(&p->b) != cudaSuccess) {
+        delete p;
+        return;
+    }
+    cudaEventRecord(p->a, s);
+    *token = p;
+}
+
+void timing_end(void *token, cudaStream_t s) {
+    if (!token) return;
+    PendingTiming *p = static_cast<PendingTiming *>(token);
+    cudaEventRecord(p->b, s);
+    std::lock_guard<std::mutex> g(g_tmu);
+    g_pending.push_back(*p);
+    delete p;
+}
+
+}  // namespace dfcsr
+
+extern "C" void dfcsr_timing_enable(int on) { dfcsr::g_timing = on != 0; }
+
+extern "C" int dfcsr_timing_collect(void) {
+    using namespace dfcsr;
+    std::lock_guard<std::mutex> g(g_tmu);
+    for (auto &p : g_pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            auto &t = g_totals[p.name];
+            t.first += ms;
+            t.second += 1;
+        }
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    g_pending.clear();
+    return DFCSR_OK;
+}
+
+extern "C" int dfcsr_timing_get(const char *name, double *total_ms, long long *launches) {
+    using namespace dfcsr;
+    std::lock_guard<std::mutex> g(g_tmu);
+    auto it = g_totals.find(name ? name : "");
+    *total_ms = (it == g_totals.end()) ? 0.0 : it->second.first;
+    *launches = (it == g_totals.end()) ? 0 : it->second.second;
+    return DFCSR_OK;
+}
+
+extern "C" void dfcsr_timing_reset(void) {
+    using namespace dfcsr;
+    std::lock_guard<std::mutex> g(g_tmu);
+    for (auto &p : g_pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    g_pending.clear();
+    g_totals.clear();
+}

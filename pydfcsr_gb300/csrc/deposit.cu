@@ -370,6 +370,7 @@ extern "C" int dfcsr_beam_moments(const double *x, const double *z, int64_t n, d
     }
     cudaStream_t s = as_stream(stream);
     double *part = reinterpret_cast<double *>(workspace);
+    ScopedTiming tm("beam_moments", s);
     DFCSR_CUDA_TRY(cudaMemsetAsync(out, 0, 16 * sizeof(double), s));
     moments_pass<1><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
     moments_finish<1><<<1, MOM_THREADS, 0, s>>>(part, nblk, n, out);
@@ -406,6 +407,7 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
                     (long long)n);
     DFCSR_CHECK_ARG(n == 0 || (q1 && q2), "dfcsr_deposit_cic2d: null coordinates");
     DFCSR_CHECK_ARG(end1 != start1 && end2 != start2, "dfcsr_deposit_cic2d: empty bin range");
+    DFCSR_CHECK_ARG(!(out1 && n > 0 && !w1), "dfcsr_deposit_cic2d: out1 given without w1");
     cudaStream_t s = as_stream(stream);
     const DepositLayout L = deposit_layout(n, nb1, nb2);
     Carver c{reinterpret_cast<char *>(workspace), workspace_bytes, 0};
@@ -420,6 +422,7 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
     const double inv2 = 1.0 / ((end2 - start2) / nb2);
     DFCSR_CUDA_TRY(cudaMemsetAsync(cs, 0, sizeof(uint32_t) * ((size_t)L.nkeys + 1), s));
     DFCSR_CUDA_TRY(cudaMemsetAsync(ce, 0, sizeof(uint32_t) * ((size_t)L.nkeys + 1), s));
+    ScopedTiming tm("deposit_cic2d", s);
     if (n > 0) {
         const int tb = 256;
         cic_keys<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(q1, q2, n, nb1, start1, inv1, nb2,
@@ -442,7 +445,7 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
         DFCSR_CUDA_TRY(cudaMemsetAsync(part, 0, sizeof(double) * (size_t)L.nkeys * 8, s));
     }
     const int64_t cells = (int64_t)nb1 * nb2;
-    cic_assemble<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(part, nb1, nb2, out0, w1 ? out1 : nullptr);
+    cic_assemble<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(part, nb1, nb2, out0, out1);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }

@@ -59,6 +59,18 @@ struct Carver {
 
 int num_sms();
 
+// Kernel timing hooks (capi.cu): no-ops unless dfcsr_timing_enable(1).
+bool timing_on();
+void timing_begin(const char *name, cudaStream_t s, void **token);
+void timing_end(void *token, cudaStream_t s);
+
+struct ScopedTiming {
+    void *tok;
+    cudaStream_t s;
+    ScopedTiming(const char *name, cudaStream_t st) : tok(nullptr), s(st) { timing_begin(name, st, &tok); }
+    ~ScopedTiming() { timing_end(tok, s); }
+};
+
 // ------------------------------------------------------------ device math
 // Reference axis rule of interpolate3D / interpolate1D: i0 = int(u)
 // (truncation toward zero), i1 = i0 unless i0 is the last index, in range iff

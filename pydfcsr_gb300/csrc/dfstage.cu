@@ -258,6 +258,7 @@ extern "C" int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, doub
     const int tb = 256, nb = (n + tb - 1) / tb;
     const double vth = p->velocity_threshold;
 
+    ScopedTiming tm("df_finalize", s);
     field_max<<<1, RED_THREADS, 0, s>>>(density, n, sc + 5);
     threshold_divide<<<nb, tb, 0, s>>>(density, vx, n, sc, vth);
     launch_sg(0, FieldSet{{density, vx}, {T0, T1}}, 2, nx, nz, p, s);

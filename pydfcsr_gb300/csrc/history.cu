@@ -80,6 +80,7 @@ extern "C" int dfcsr_history_regrid(const double *density, const double *density
     DFCSR_CHECK_ARG(!ring32_slot || ((uintptr_t)ring32_slot % 16) == 0,
                     "dfcsr_history_regrid: ring32 slot must be 16-byte aligned");
     const int64_t cells = (int64_t)nxi * nzi;
+    ScopedTiming tm("history_regrid", as_stream(stream));
     regrid5<<<(unsigned)((cells + 255) / 256), 256, 0, as_stream(stream)>>>(
         density, density_x, density_z, vx, vx_x, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,
         vx_x_fill, ring64_slot, ring32_slot);

@@ -140,6 +140,7 @@ extern "C" int dfcsr_wake_fp64(const dfcsr_wake_job *jobs, const int32_t *job_of
     DFCSR_CHECK_ARG(jobs && s && x && dE && xkick, "dfcsr_wake_fp64: null pointer");
     cudaStream_t st = as_stream(stream);
     const int64_t grid64 = n < (int64_t)(1 << 30) ? n : (int64_t)(1 << 30);
+    ScopedTiming tm("wake_fp64", st);
     wake_fp64_kernel<<<(unsigned)grid64, F64_THREADS, 0, st>>>(jobs, job_of_point, s, x, n, dE, xkick);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;

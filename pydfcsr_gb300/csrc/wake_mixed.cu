@@ -504,14 +504,22 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
     for (int64_t first = 0; first < n; first += L.batch) {
         const int64_t count = (n - first < L.batch) ? n - first : L.batch;
         DFCSR_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
-        mixed_geometry<<<dim3((unsigned)count, WAKE_MAX_REGIONS), GEO_THREADS, 0, st>>>(
-            jobs, job_of_point, s, x, first, count, L.rec_words, rec, meta, obs_vx);
+        {
+            ScopedTiming tm("wake_mixed_geometry", st);
+            mixed_geometry<<<dim3((unsigned)count, WAKE_MAX_REGIONS), GEO_THREADS, 0, st>>>(
+                jobs, job_of_point, s, x, first, count, L.rec_words, rec, meta, obs_vx);
+        }
         const int blocks = (int)((int64_t)blocks_max < count ? blocks_max : count);
-        mixed_integral<<<blocks, MX_THREADS, sizeof(IntegralSmem), st>>>(
-            jobs, job_of_point, first, count, L.rec_words, rec, meta, part, counter);
-        if (use_band)
+        {
+            ScopedTiming tm("wake_mixed_integral", st);
+            mixed_integral<<<blocks, MX_THREADS, sizeof(IntegralSmem), st>>>(
+                jobs, job_of_point, first, count, L.rec_words, rec, meta, part, counter);
+        }
+        if (use_band) {
+            ScopedTiming tm("wake_mixed_band", st);
             mixed_band<<<dim3((unsigned)count, WAKE_MAX_REGIONS), 128, 0, st>>>(
                 jobs, job_of_point, s, x, first, count, meta, obs_vx, band);
+        }
         mixed_finalize<<<(unsigned)((count + 127) / 128), 128, 0, st>>>(
             jobs, job_of_point, first, count, meta, part, use_band ? band : nullptr, dE, xkick);
     }

@@ -335,7 +335,7 @@ class DF_tracker:
         iz, wz, oz = rgi_axis(entry.z_grids, self.z_grid_interp)
         nxi, nzi = ix.size, iz.size
         # pack the index tables into one copy: int32 idx | f64 w | u8 oob
-        blob = np.zeros(8 * (2 * nxi + 2 * nzi) + 2 * (nxi + nzi) + 64, dtype=np.uint8)
+        blob = np.zeros(13 * (nxi + nzi) + 6 * 16 + 32, dtype=np.uint8)
         o = 0
         views = []
         for arr in (wx, wz, ix, iz, ox, oz):
