@@ -137,8 +137,9 @@ int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, double *vx,
  * ix[nxi], wx[nxi], oobx[nxi] (1 = outside), iz[nzi], wz[nzi], oobz[nzi].
  * vx_x_fill is a DEVICE pointer to the fill value of vx_x (its mean).
  * ring64: [slot][nxi][nzi][5] doubles (or NULL); ring32: [slot][nxi][nzi][8]
- * floats, fields 0..4 used (or NULL).  Field order: density, density_x,
- * density_z, vx, vx_x.
+ * floats (or NULL): fields 0..4, then in slot 5 the low part of density_x
+ * (density_x - (double)(float)density_x), slots 6..7 zero.  Field order:
+ * density, density_x, density_z, vx, vx_x.
  */
 int dfcsr_history_regrid(const double *density, const double *density_x,
                          const double *density_z, const double *vx,
@@ -172,7 +173,7 @@ int dfcsr_interp1d(const double *q, int64_t m, const double *table, int n,
  */
 typedef struct {
     const double *ring64;       /* [cap][nx][nz][5] or NULL                   */
-    const float *ring32;        /* [cap][nx][nz][8] or NULL                   */
+    const float *ring32;        /* [cap][nx][nz][8] or NULL (see regrid)      */
     int cap, head, nt, nx, nz;  /* ring capacity, oldest slot, slices, grid   */
     int pad0;
     double t_min, x_min, z_min; /* build_interpolant (deposit.py:416-421)     */

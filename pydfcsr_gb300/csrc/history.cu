@@ -53,9 +53,15 @@ __global__ void regrid5(const double *__restrict__ f0, const double *__restrict_
         for (int q = 0; q < 5; ++q) o[q] = v[q];
     }
     if (out32) {
+        // FP32 cell: density, density_x (high part), density_z, vx | vx_x,
+        // density_x low part (v - (double)hi), 0, 0.  density_x is carried as
+        // a float-float pair: its integral over x' cancels to ~1e-4 of its
+        // magnitude in the far region, so it needs ~48 bits.
         float4 *o = reinterpret_cast<float4 *>(out32 + (size_t)t * 8);
-        o[0] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
-        o[1] = make_float4((float)v[4], 0.f, 0.f, 0.f);
+        const float hi = (float)v[1];
+        const float lo = (float)(v[1] - (double)hi);
+        o[0] = make_float4((float)v[0], hi, (float)v[2], (float)v[3]);
+        o[1] = make_float4((float)v[4], lo, 0.f, 0.f);
     }
 }
 

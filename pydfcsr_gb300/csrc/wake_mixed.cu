@@ -135,7 +135,7 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         put_f(cb, C_G, cs, j, g);
         put_f(cb, C_H, cs, j, h);
         put_f(cb, C_K0X, cs, j, bb - a * e);
-        put_f(cb, C_K1X, cs, j, a * g + bb * e);
+        put_f(cb, C_K1X, cs, j, (a * g - 1.0) + bb * e);   // K1x - 1 (K1x ~ 1)
         put_f(cb, C_K2X, cs, j, bb * g);
         put_f(cb, C_K0Z, cs, j, a * (1.0 - h));
         put_f(cb, C_K1Z, cs, j, a * e + bb * h);
@@ -186,44 +186,73 @@ struct Fields5 {
     float den, dx, dz, vx, vxx;
 };
 
-__device__ __forceinline__ void load5(const float *p, float4 &v, float &w) {
-    v = __ldg(reinterpret_cast<const float4 *>(p));
-    w = __ldg(p + 4);
+// Error-free transformations (round-to-nearest intrinsics: never contracted).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// Trilinear FP32 gather of the five fields from ring32 [slot][nx][nz][8]:
-// interpolate t, then x, then z (reference order).
+// Linear interpolation a + w (b - a) of float-float values (hi, lo).
+__device__ __forceinline__ float2 lerp_ff(float2 A, float2 B, float w) {
+    float dh, de;
+    two_sum(B.x, -A.x, dh, de);
+    const float dl = __fadd_rn(de, __fsub_rn(B.y, A.y));
+    const float ph = __fmul_rn(w, dh);
+    const float pe = __fmaf_rn(w, dh, -ph);
+    const float pl = __fmaf_rn(w, dl, pe);
+    float rh, re;
+    two_sum(A.x, ph, rh, re);
+    const float rl = __fadd_rn(re, __fadd_rn(A.y, pl));
+    const float s = __fadd_rn(rh, rl);
+    return make_float2(s, __fsub_rn(rl, __fsub_rn(s, rh)));
+}
+
+// a + w (b - a) with one rounding for the product-add.
+__device__ __forceinline__ float lerp1(float a, float b, float w) { return fmaf(w, b - a, a); }
+
+// Trilinear FP32 gather of the five fields from ring32 [slot][nx][nz][8]
+// (cell: den, dx_hi, dz, vx | vxx, dx_lo, 0, 0), interpolating t, then x,
+// then z like the reference; density_x in float-float.
 __device__ __forceinline__ Fields5 gather5(const float *__restrict__ ring, int nx, int nz, int s0, int s1,
                                            float td, int x0, int x1, float xd, int z0, int z1, float zd) {
     const size_t nxz = (size_t)nx * nz;
     const size_t dz8 = (size_t)(z1 - z0) * 8;
-    const float *p00 = ring + ((size_t)s0 * nxz + (size_t)x0 * nz + z0) * 8;
-    const float *q00 = ring + ((size_t)s1 * nxz + (size_t)x0 * nz + z0) * 8;
-    const float *p10 = ring + ((size_t)s0 * nxz + (size_t)x1 * nz + z0) * 8;
-    const float *q10 = ring + ((size_t)s1 * nxz + (size_t)x1 * nz + z0) * 8;
-    float4 A0, A1, B0, B1, C0, C1, D0, D1;
-    float a0, a1, b0, b1, c0, c1, d0, d1;
-    load5(p00, A0, a0); load5(p00 + dz8, A1, a1);
-    load5(q00, B0, b0); load5(q00 + dz8, B1, b1);
-    load5(p10, C0, c0); load5(p10 + dz8, C1, c1);
-    load5(q10, D0, d0); load5(q10 + dz8, D1, d1);
-    const float ut = 1.f - td, ux = 1.f - xd, uz = 1.f - zd;
+    const float4 *p00 = reinterpret_cast<const float4 *>(ring + ((size_t)s0 * nxz + (size_t)x0 * nz + z0) * 8);
+    const float4 *q00 = reinterpret_cast<const float4 *>(ring + ((size_t)s1 * nxz + (size_t)x0 * nz + z0) * 8);
+    const float4 *p10 = reinterpret_cast<const float4 *>(ring + ((size_t)s0 * nxz + (size_t)x1 * nz + z0) * 8);
+    const float4 *q10 = reinterpret_cast<const float4 *>(ring + ((size_t)s1 * nxz + (size_t)x1 * nz + z0) * 8);
+    const size_t dz4 = dz8 / 4;
+    // corner order: [x][z][t]
+    const float4 A0 = __ldg(p00), a0 = __ldg(p00 + 1), A1 = __ldg(p00 + dz4), a1 = __ldg(p00 + dz4 + 1);
+    const float4 B0 = __ldg(q00), b0 = __ldg(q00 + 1), B1 = __ldg(q00 + dz4), b1 = __ldg(q00 + dz4 + 1);
+    const float4 C0 = __ldg(p10), c0 = __ldg(p10 + 1), C1 = __ldg(p10 + dz4), c1 = __ldg(p10 + dz4 + 1);
+    const float4 D0 = __ldg(q10), d0 = __ldg(q10 + 1), D1 = __ldg(q10 + dz4), d1 = __ldg(q10 + dz4 + 1);
     auto tri = [&](float v00a, float v00b, float v01a, float v01b, float v10a, float v10b,
                    float v11a, float v11b) -> float {
-        const float c00 = v00a * ut + v00b * td;
-        const float c01 = v01a * ut + v01b * td;
-        const float c10 = v10a * ut + v10b * td;
-        const float c11 = v11a * ut + v11b * td;
-        const float e0 = c00 * ux + c10 * xd;
-        const float e1 = c01 * ux + c11 * xd;
-        return e0 * uz + e1 * zd;
+        const float c00 = lerp1(v00a, v00b, td);
+        const float c01 = lerp1(v01a, v01b, td);
+        const float c10 = lerp1(v10a, v10b, td);
+        const float c11 = lerp1(v11a, v11b, td);
+        const float e0 = lerp1(c00, c10, xd);
+        const float e1 = lerp1(c01, c11, xd);
+        return lerp1(e0, e1, zd);
     };
     Fields5 r;
     r.den = tri(A0.x, B0.x, A1.x, B1.x, C0.x, D0.x, C1.x, D1.x);
-    r.dx = tri(A0.y, B0.y, A1.y, B1.y, C0.y, D0.y, C1.y, D1.y);
     r.dz = tri(A0.z, B0.z, A1.z, B1.z, C0.z, D0.z, C1.z, D1.z);
     r.vx = tri(A0.w, B0.w, A1.w, B1.w, C0.w, D0.w, C1.w, D1.w);
-    r.vxx = tri(a0, b0, a1, b1, c0, d0, c1, d1);
+    r.vxx = tri(a0.x, b0.x, a1.x, b1.x, c0.x, d0.x, c1.x, d1.x);
+    {
+        const float2 c00 = lerp_ff(make_float2(A0.y, a0.y), make_float2(B0.y, b0.y), td);
+        const float2 c01 = lerp_ff(make_float2(A1.y, a1.y), make_float2(B1.y, b1.y), td);
+        const float2 c10 = lerp_ff(make_float2(C0.y, c0.y), make_float2(D0.y, d0.y), td);
+        const float2 c11 = lerp_ff(make_float2(C1.y, c1.y), make_float2(D1.y, d1.y), td);
+        const float2 e0 = lerp_ff(c00, c10, xd);
+        const float2 e1 = lerp_ff(c01, c11, xd);
+        const float2 f = lerp_ff(e0, e1, zd);
+        r.dx = __fadd_rn(f.x, f.y);
+    }
     return r;
 }
 
@@ -303,7 +332,9 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
                     }
                     const float scale = 1.f + sm.row[R_XP][i] * sm.col[C_RHO][jl];
                     const float vr = F.vx;
-                    const float brx = sm.col[C_K0X][jl] - vr * (sm.col[C_K1X][jl] + vr * sm.col[C_K2X][jl]);
+                    // K1x ~ 1 is stored as K1x - 1 so that K0x - vx' (nearly equal
+                    // transverse velocities) is formed exactly
+                    const float brx = (sm.col[C_K0X][jl] - vr) - vr * (sm.col[C_K1X][jl] + vr * sm.col[C_K2X][jl]);
                     const float brz = sm.col[C_K0Z][jl] - vr * (sm.col[C_K1Z][jl] + vr * sm.col[C_K2Z][jl]);
                     const float p1 = sm.col[C_A][jl] + vr * sm.col[C_B][jl];
                     const float num = scale * F.dx * brx + F.dz * brz - scale * p1 * F.den * F.vxx;

@@ -94,8 +94,9 @@ class HistoryRing:
     """Device ring of (slot, x, z) grids holding the five DF fields per cell.
 
     ``ring64`` is float64 [cap, nx, nz, 5] (plain FP64 wake); ``ring32`` is
-    float32 [cap, nx, nz, 8] with fields 0..4 used (mixed-precision wake;
-    32-byte cells so a corner's fields load as two aligned float4).  Logical
+    float32 [cap, nx, nz, 8] (mixed-precision wake): fields 0..4, the low part
+    of density_x in slot 5 (density_x is carried as a float-float pair), 32-byte
+    cells so a corner loads as two aligned float4.  Logical
     slice k (0 = oldest) lives in physical slot (head + k) % cap.
     """
 

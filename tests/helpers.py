@@ -24,6 +24,32 @@ def rel_err(a, b):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-3 * peak)))
 
 
+def wake_errors(dE, xk, dE_ref, xk_ref):
+    """Error of a wake (dE/dct, x-kick) against a reference wake.
+
+    Both components share the unit (MeV/m); S is the peak of the reference
+    wake over the mesh and both components.
+      max_rel       max |a - b| / S
+      rms_rel       ||a - b||_2 / ||b||_2 over the mesh and both components
+      pointwise_dE  max |a - b| / max(|b|, 1e-3 S) for dE/dct  (diagnostic)
+      pointwise_xk  the same for the x-kick                     (diagnostic)
+    """
+    dE, xk, dE_ref, xk_ref = (np.asarray(v, float).ravel() for v in (dE, xk, dE_ref, xk_ref))
+    a = np.concatenate([dE, xk])
+    b = np.concatenate([dE_ref, xk_ref])
+    S = float(np.max(np.abs(b)))
+    if S == 0:
+        S = 1.0
+    nb = float(np.sqrt(np.sum(b * b))) or 1.0
+    floor = 1e-3 * S
+    return {
+        "max_rel": float(np.max(np.abs(a - b)) / S),
+        "rms_rel": float(np.sqrt(np.sum((a - b) ** 2)) / nb),
+        "pointwise_dE": float(np.max(np.abs(dE - dE_ref) / np.maximum(np.abs(dE_ref), floor))),
+        "pointwise_xk": float(np.max(np.abs(xk - xk_ref) / np.maximum(np.abs(xk_ref), floor))),
+    }
+
+
 def rms_rel(a, b):
     a, b = np.asarray(a, float), np.asarray(b, float)
     nb = np.sqrt(np.mean(b * b))
