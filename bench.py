@@ -245,9 +245,11 @@ def gpu_arm(a):
     dev_ms = e0.elapsed_time(e1)
     kname = "wake_mixed_integral" if a.precision == "mixed" else "wake_fp64"
     k_ms, k_n = _lib.timing_read(kname)
-    launches = {n: _lib.timing_read(n)[1] for n in
-                ("beam_moments", "deposit_cic2d", "df_finalize", "history_regrid", "wake_fp64",
-                 "wake_mixed_geometry", "wake_mixed_integral", "wake_mixed_band")}
+    names = ("beam_moments", "deposit_cic2d", "df_finalize", "history_regrid", "wake_fp64",
+             "wake_mixed_geometry", "wake_mixed_integral", "wake_mixed_band")
+    kt = {n: _lib.timing_read(n) for n in names}
+    launches = {n: v[1] for n, v in kt.items()}
+    kernel_ms = {n: round(v[0] / K, 4) for n, v in kt.items() if v[1]}
     step_ms = dev_ms / K
     if world > 1:
         t = torch.tensor([step_ms], device="cuda")
@@ -299,6 +301,7 @@ def gpu_arm(a):
                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
     out["gpu_launches"] = int(sum(launches.values()))
     out["kernel_launches_by_name"] = launches
+    out["kernel_ms_per_step"] = kernel_ms
 
     # plain FP64 leg on the same steps (for the mixed vs FP64 speed-up)
     if not a.no_fp64 and a.precision == "mixed":
