@@ -92,6 +92,25 @@ int dfcsr_deposit_cic2d(const double *q1, const double *q2, const double *w0,
                         double *out0, double *out1,
                         void *workspace, size_t workspace_bytes, void *stream);
 
+/* Deposit that allocates nothing.  No counterpart in the reference.  For
+ * callers that cannot allocate device memory when they deposit (a host code
+ * that plans its device buffers up front and forbids allocation inside its
+ * step loop, a plugin host whose memory belongs to its own pool): the
+ * scratch is one fixed device array inside the library (24 MiB, reserved on
+ * every GPU that loads this entry point, held until exit).  Same arguments
+ * and results as dfcsr_deposit_cic2d without the workspace.  Limits: at most
+ * 1,048,576 particles and (nb1 + 1) * (nb2 + 1) <= 257 * 257 (a 256 x 256
+ * grid); larger requests return DFCSR_BAD_ARG.  The first call on a device
+ * resolves the array's device address (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+size_t dfcsr_deposit_noalloc_max_bytes(void);
+int dfcsr_deposit_cic2d_noalloc(const double *q1, const double *q2, const double *w0,
+                                const double *w1, int64_t n,
+                                int nb1, double start1, double end1,
+                                int nb2, double start2, double end2,
+                                double *out0, double *out1, void *stream);
+
 /* ------------------------------------------------------------------------
  * Distribution-function finalisation: everything get_DF does after the two
  * deposits (deposit.py:183-235), in place on device arrays [nx][nz]:

@@ -28,6 +28,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "capi.cu": [],
     "deposit.cu": [],
+    "deposit_noalloc.cu": [],
     "dfstage.cu": [],
     "history.cu": [],
     "interp.cu": [],
