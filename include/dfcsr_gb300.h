@@ -230,7 +230,8 @@ int dfcsr_wake_integrand(const dfcsr_wake_job *job, double s, double x,
 /* Mixed precision: FP64 per-(point, s') retarded geometry written as
  * per-column records, FP32 gathers and integrand with history coordinates
  * carried as integer cell + FP32 offset, Kahan-compensated FP32 sums reduced
- * in FP64 (fixed order).  Needs ring32 in every job.  xbins_max / zbins_max
+ * in FP64 (fixed order).  Needs ring32 in every job (below 64 GiB: cells are
+ * addressed with 32-bit offsets).  xbins_max / zbins_max
  * bound the integration bins of all jobs in the call.  use_band != 0 runs
  * the s' columns with |s' - s| < job.near_band through the FP64 integrand.
  * Scratch: dfcsr_wake_workspace_bytes(xbins_max, zbins_max, n); points are

@@ -39,6 +39,8 @@ def wake_job(tracker, lattice, position, sigma_z, sigma_x, slope0, mean_x, forma
     tab, rho, dist = lattice.device_tables()
     j = _lib.WakeJob()
     jf = tracker.job_fields()
+    if jf["ring32"] is not None and jf["cap"] * jf["nx"] * jf["nz"] * 2 >= 2 ** 32:
+        raise ValueError("FP32 history ring too large for 32-bit cell offsets (>= 64 GiB)")
     j.ring64 = jf["ring64"]
     j.ring32 = jf["ring32"]
     for k in ("cap", "head", "nt", "nx", "nz"):
@@ -128,7 +130,7 @@ class CSR2D:
     def initialization(self):
         """Deposit the initial beam (CSR.py:70-81)."""
         b = self.beam
-        self.DF_tracker.get_DF(x=b.x, z=b.z, px=b.px, t=b.position)
+        self.DF_tracker.get_DF(x=b.x, z=b.z, px=b.px, t=b.position, moments=b._moments)
         self.DF_tracker.append_DF()
         self.DF_tracker.append_interpolant(formation_length=float("inf"),
                                            n_formation_length=self.integration_params.n_formation_length)
@@ -147,7 +149,8 @@ class CSR2D:
             self.formation_length = formation_length
         b = self.beam
         t = self.DF_tracker
-        t.get_DF(x=b.x, z=b.z, px=b.px, t=b.position)
+        # the beam's moments are of these same (x, z) tensors
+        t.get_DF(x=b.x, z=b.z, px=b.px, t=b.position, moments=b._moments)
         t.append_DF()
         t.append_interpolant(formation_length=self.formation_length,
                              n_formation_length=self.integration_params.n_formation_length)

@@ -1,21 +1,25 @@
 // Mixed-precision CSR wake (FP32 bulk, FP64 retarded geometry).
 //
 // Same integral as get_CSR_wake / get_CSR_integrand (pyDFCSR_2D/CSR.py:454-782),
-// restructured so that FP32 is safe:
-//  * geometry kernel (FP64), one thread per (observation point, region, s'
-//    column): orbit tables at s', separation R0 = r - r' at a reference x'
-//    (the region centre), |R0|, the history coordinates of t_ret and
+// restructured so that FP32 is safe and little work is wasted:
+//  * geometry kernel (FP64), one CTA per (observation point, region): per s'
+//    column the orbit tables at s', the separation R0 = r - r' at a reference
+//    x' (the region centre), |R0|, the history coordinates of t_ret and
 //    s' - t_ret, and every direction product whose difference would cancel in
-//    FP32 (v.tau', v.n', 1 - |tau'|^2, (r - r').(n - n'), ...).  Records are
+//    FP32 (v.tau', v.n', 1 - |tau'|^2, |n'|^2 - 1, (r - r').(n - n'), ...);
+//    per x' row the history x cell and the trapz weight, and the range of rows
+//    whose x' lies inside the history grid (outside it every field, hence the
+//    integrand, is exactly zero, so those rows are skipped).  Records are
 //    written for a batch of points small enough to stay resident in L2.
-//  * integral kernel (FP32), one persistent CTA loop over points: per
-//    (x', s') only an FP32 correction remains,
+//  * integral kernel (FP32), a persistent CTA loop over points: per (x', s')
+//    only an FP32 correction remains,
 //        |r - r'| = r0 + delta,  delta = D / (r0 + sqrt(r0^2 + D)),
 //        D = u (|n'|^2 u - 2 R0.n'),  u = x' - x'_ref   (no cancellation);
 //    history coordinates are an integer cell (from FP64) plus an FP32
 //    offset, so a grid index near 1000 keeps ~1e-7 cell resolution; gathers
-//    and the integrand are FP32 with Kahan-compensated per-thread sums and a
-//    fixed-order FP64 block reduction.
+//    and the integrand are FP32 (density_x as a float-float pair in the far
+//    region, where its x' integral cancels), Kahan-compensated per-thread sums
+//    and a fixed-order FP64 block reduction.
 //  * band kernel (FP64, optional): s' columns with |s' - s| < near_band are
 //    skipped by the integral kernel and evaluated with the FP64 integrand.
 //  * finalize kernel: adds the regions in the reference's order and scales.
@@ -29,13 +33,18 @@ constexpr int MX_MAX_ROWS = 1024;   // x' rows per region (2 * xbins)
 constexpr int MX_MAX_COLS = 4096;   // s' columns per region (zbins)
 constexpr int GEO_THREADS = 128;
 
-// column record: 24 words (SoA within a region)
-enum ColField {
-    C_TB, C_ZB, C_TF, C_ZF, C_R0, C_BG, C_CG, C_A, C_B, C_E, C_G, C_H,
-    C_K0X, C_K1X, C_K2X, C_K0Z, C_K1Z, C_K2Z, C_Q0, C_Q1, C_Q2, C_M0, C_RHO, C_WS, C_NF
-};
-// row record: 5 words
-enum RowField { R_XB, R_XF, R_U, R_XP, R_WX, R_NF };
+// Column record: 28 words (7 float4; stride 112 B keeps 8-lane phases of
+// 16-byte shared loads conflict free).  Row record: 8 words (2 float4).
+constexpr int CW = 28;
+constexpr int RW = 8;
+// column record words (float4 groups):
+//  0: t cell (int), z cell (int), t offset, z offset
+//  1: |R0|, R0.n', |n'|^2 - 1, curvature at s'
+//  2: v.tau' (a), v.n' (b), tau'.n' (e), |n'|^2 (g)
+//  3: |tau'|^2 (h), K0x = b - a e, K1x - 1 = a g - 1 + b e, K2x = b g
+//  4: K0z = a (1 - h), K1z = a e + b h, K2z = b e, Q0 = R0.(n - n')
+//  5: Q1 = n'.(n - n'), q2 = n.tau', M0 = Q0 - q2 |R0|, trapz weight in s'
+// row record words: x cell (int), x offset, u = x' - x'_ref, x' | trapz weight in x'
 
 struct RegionMeta {
     int nxp, nsp, col_off, row_off;   // offsets in words within the point record
@@ -46,26 +55,58 @@ struct PointMeta {
     RegionMeta reg[WAKE_MAX_REGIONS];
 };
 
-// Per-point record size (words) for a job: 4 regions of zbins columns and at
-// most 5 * xbins rows in total.
+// Per-point record size (words): 4 regions of zbins columns and at most
+// 5 * xbins rows in total.
 __host__ __device__ inline size_t point_record_words(int xbins, int zbins) {
-    return (size_t)WAKE_MAX_REGIONS * zbins * C_NF + (size_t)5 * xbins * R_NF;
+    return (size_t)WAKE_MAX_REGIONS * zbins * CW + (size_t)5 * xbins * RW;
 }
 
-__device__ __forceinline__ void put_i(float *base, int field, int stride, int idx, int v) {
-    base[(size_t)field * stride + idx] = __int_as_float(v);
-}
-__device__ __forceinline__ void put_f(float *base, int field, int stride, int idx, double v) {
-    base[(size_t)field * stride + idx] = (float)v;
-}
 __device__ __forceinline__ int clamp_int(double v) { return (int)fmax(fmin(v, 2.0e9), -2.0e9); }
+
+// s' of column j and x' of row i: start + k * step (the reference's
+// linspace up to rounding, which the mixed path does not need to reproduce).
+struct Axis {
+    double start, step;
+    int n;
+    __device__ double at(int k) const { return fma((double)k, step, start); }
+    __device__ double weight(int k) const {   // trapz weight of sample k
+        if (n < 2) return 0.0;
+        return (k == 0 || k == n - 1) ? 0.5 * step : step;
+    }
+};
+
+__device__ __forceinline__ Axis make_axis(double a, double b, int n) {
+    Axis ax;
+    ax.start = a;
+    ax.n = n;
+    ax.step = (n > 1) ? (b - a) / (double)(n - 1) : 0.0;
+    return ax;
+}
+
+__device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *rm, bool &ok,
+                                       size_t rec_words) {
+    int off = 0;
+    ok = true;
+    for (int k = 0; k < nreg; ++k) {
+        rm[k].nxp = reg[k].nxp;
+        rm[k].nsp = reg[k].nsp;
+        rm[k].col_off = off;
+        off += reg[k].nsp * CW;
+        rm[k].row_off = off;
+        off += reg[k].nxp * RW;
+        if (reg[k].nxp < 1 || reg[k].nxp > MX_MAX_ROWS || reg[k].nsp < 1 || reg[k].nsp > MX_MAX_COLS)
+            ok = false;
+    }
+    if ((size_t)off > rec_words) ok = false;
+}
 
 // grid (points in batch, regions); block GEO_THREADS over columns then rows.
 __global__ void __launch_bounds__(GEO_THREADS)
 mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
                const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
                size_t rec_words, float *__restrict__ rec, PointMeta *__restrict__ meta,
-               double *__restrict__ obs_vx) {
+               int2 *__restrict__ rows_valid, double *__restrict__ obs_vx) {
+    __shared__ int s_lo, s_hi;
     const int64_t b = blockIdx.x;
     const int64_t pt = first + b;
     const int r = blockIdx.y;
@@ -74,22 +115,9 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
     const double t = J.position, s = S[pt], x = X[pt];
     Region reg[WAKE_MAX_REGIONS];
     const int nreg = wake_regions(J, s, x, reg);
-    float *base = rec + (size_t)b * rec_words;
-    // layout offsets (same computation in every block of this point)
-    int off = 0;
     RegionMeta rm[WAKE_MAX_REGIONS];
-    bool ok = true;
-    for (int k = 0; k < nreg; ++k) {
-        rm[k].nxp = reg[k].nxp;
-        rm[k].nsp = reg[k].nsp;
-        rm[k].col_off = off;
-        off += reg[k].nsp * C_NF;
-        rm[k].row_off = off;
-        off += reg[k].nxp * R_NF;
-        if (reg[k].nxp < 1 || reg[k].nxp > MX_MAX_ROWS || reg[k].nsp < 1 || reg[k].nsp > MX_MAX_COLS)
-            ok = false;
-    }
-    if ((size_t)off > rec_words) ok = false;
+    bool ok;
+    layout(reg, nreg, rm, ok, rec_words);
     if (r == 0 && threadIdx.x == 0) {
         PointMeta m;
         m.nreg = nreg;
@@ -105,68 +133,77 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
     lattice_lerp(J, s, lat_s);
     const double X0s = lat_s[0], Y0s = lat_s[1], nsx = lat_s[2], nsy = lat_s[3];
     const double vxo = lat_s[4] + vx_obs * nsx, vyo = lat_s[5] + vx_obs * nsy;
-    const double xref = np_linspace_at(R.xl, R.xr, R.nxp, R.nxp / 2);
-    float *cb = base + rm[r].col_off;
-    const int cs = R.nsp;
+    const Axis ax_s = make_axis(R.sl, R.sr, R.nsp);
+    const Axis ax_x = make_axis(R.xl, R.xr, R.nxp);
+    const double xref = ax_x.at(R.nxp / 2);
+    const double inv_s = 1.0 / J.s_delta, inv_t = 1.0 / J.t_delta, inv_z = 1.0 / J.z_delta;
+    const double inv_x = 1.0 / J.x_delta;
+    float4 *cb = reinterpret_cast<float4 *>(rec + (size_t)b * rec_words + rm[r].col_off);
     for (int j = threadIdx.x; j < R.nsp; j += blockDim.x) {
-        const double spj = np_linspace_at(R.sl, R.sr, R.nsp, j);
+        const double spj = ax_s.at(j);
+        // orbit tables at s' (interpolate1D rule, index by multiplication)
         double L[6];
-        lattice_lerp(J, spj, L);
+        {
+            int a0, a1;
+            double f;
+            if (axis_index((spj - J.s_min) * inv_s, J.nsample, a0, a1, f)) {
+                const double *pa = J.lattice + (size_t)a0 * 6, *pb = J.lattice + (size_t)a1 * 6;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) L[k] = fma(f, pb[k] - pa[k], pa[k]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 6; ++k) L[k] = 0.0;
+            }
+        }
         const double npx = L[2], npy = L[3], tpx = L[4], tpy = L[5];
         const double Ax = X0s - L[0] + x * nsx, Ay = Y0s - L[1] + x * nsy;
         const double rx0 = Ax - xref * npx, ry0 = Ay - xref * npy;
         const double r0 = sqrt(rx0 * rx0 + ry0 * ry0);
-        const double ut0 = (t - r0 - J.t_min) / J.t_delta;
-        const double uz0 = (spj - (t - r0) - J.z_min) / J.z_delta;
+        const double ut0 = (t - r0 - J.t_min) * inv_t;
+        const double uz0 = (spj - (t - r0) - J.z_min) * inv_z;
         const double tfl = floor(ut0), zfl = floor(uz0);
-        put_i(cb, C_TB, cs, j, clamp_int(tfl));
-        put_i(cb, C_ZB, cs, j, clamp_int(zfl));
-        put_f(cb, C_TF, cs, j, ut0 - tfl);
-        put_f(cb, C_ZF, cs, j, uz0 - zfl);
-        put_f(cb, C_R0, cs, j, r0);
-        put_f(cb, C_BG, cs, j, rx0 * npx + ry0 * npy);
-        put_f(cb, C_CG, cs, j, npx * npx + npy * npy);
         const double a = vxo * tpx + vyo * tpy, bb = vxo * npx + vyo * npy;
         const double e = tpx * npx + tpy * npy, g = npx * npx + npy * npy;
         const double h = tpx * tpx + tpy * tpy;
-        put_f(cb, C_A, cs, j, a);
-        put_f(cb, C_B, cs, j, bb);
-        put_f(cb, C_E, cs, j, e);
-        put_f(cb, C_G, cs, j, g);
-        put_f(cb, C_H, cs, j, h);
-        put_f(cb, C_K0X, cs, j, bb - a * e);
-        put_f(cb, C_K1X, cs, j, (a * g - 1.0) + bb * e);   // K1x - 1 (K1x ~ 1)
-        put_f(cb, C_K2X, cs, j, bb * g);
-        put_f(cb, C_K0Z, cs, j, a * (1.0 - h));
-        put_f(cb, C_K1Z, cs, j, a * e + bb * h);
-        put_f(cb, C_K2Z, cs, j, bb * e);
         const double nmx = nsx - npx, nmy = nsy - npy;
         const double Q0 = rx0 * nmx + ry0 * nmy;
         const double q2 = nsx * tpx + nsy * tpy;
-        put_f(cb, C_Q0, cs, j, Q0);
-        put_f(cb, C_Q1, cs, j, npx * nmx + npy * nmy);
-        put_f(cb, C_Q2, cs, j, q2);
-        put_f(cb, C_M0, cs, j, Q0 - q2 * r0);
-        put_f(cb, C_RHO, cs, j, rho_at(J, spj));
-        const double dl = (j > 0) ? spj - np_linspace_at(R.sl, R.sr, R.nsp, j - 1) : 0.0;
-        const double dr = (j < R.nsp - 1) ? np_linspace_at(R.sl, R.sr, R.nsp, j + 1) - spj : 0.0;
         const bool near = J.near_band > 0.0 && fabs(spj - s) < J.near_band;
-        put_f(cb, C_WS, cs, j, near ? 0.0 : 0.5 * (dl + dr));   // band columns: FP64 kernel
+        float4 *o = cb + (size_t)j * (CW / 4);
+        o[0] = make_float4(__int_as_float(clamp_int(tfl)), __int_as_float(clamp_int(zfl)),
+                           (float)(ut0 - tfl), (float)(uz0 - zfl));
+        o[1] = make_float4((float)r0, (float)(rx0 * npx + ry0 * npy), (float)(g - 1.0),
+                           (float)rho_at(J, spj));
+        o[2] = make_float4((float)a, (float)bb, (float)e, (float)g);
+        o[3] = make_float4((float)h, (float)(bb - a * e), (float)((a * g - 1.0) + bb * e),
+                           (float)(bb * g));
+        o[4] = make_float4((float)(a * (1.0 - h)), (float)(a * e + bb * h), (float)(bb * e),
+                           (float)Q0);
+        o[5] = make_float4((float)(npx * nmx + npy * nmy), (float)q2, (float)(Q0 - q2 * r0),
+                           near ? 0.f : (float)ax_s.weight(j));   // band columns: FP64 kernel
     }
-    float *rb = base + rm[r].row_off;
-    const int rs = R.nxp;
+    // rows: x cell, offset, u = x' - x'_ref, x', trapz weight; valid row range
+    if (threadIdx.x == 0) { s_lo = R.nxp; s_hi = -1; }
+    __syncthreads();
+    float4 *rb = reinterpret_cast<float4 *>(rec + (size_t)b * rec_words + rm[r].row_off);
+    const double ux_first = (R.xl - J.x_min) * inv_x, dux = ax_x.step * inv_x;
+    int lo = R.nxp, hi = -1;
     for (int i = threadIdx.x; i < R.nxp; i += blockDim.x) {
-        const double xpi = np_linspace_at(R.xl, R.xr, R.nxp, i);
-        const double ux = (xpi - J.x_min) / J.x_delta;
+        const double xpi = ax_x.at(i);
+        const double ux = fma((double)i, dux, ux_first);
         const double fb = floor(ux);
-        put_i(rb, R_XB, rs, i, clamp_int(fb));
-        put_f(rb, R_XF, rs, i, ux - fb);
-        put_f(rb, R_U, rs, i, xpi - xref);
-        put_f(rb, R_XP, rs, i, xpi);
-        const double dl = (i > 0) ? xpi - np_linspace_at(R.xl, R.xr, R.nxp, i - 1) : 0.0;
-        const double dr = (i < R.nxp - 1) ? np_linspace_at(R.xl, R.xr, R.nxp, i + 1) - xpi : 0.0;
-        put_f(rb, R_WX, rs, i, 0.5 * (dl + dr));
+        rb[2 * i] = make_float4(__int_as_float(clamp_int(fb)), (float)(ux - fb), (float)(xpi - xref),
+                                (float)xpi);
+        rb[2 * i + 1] = make_float4((float)ax_x.weight(i), 0.f, 0.f, 0.f);
+        if (ux > -1.0 && ux < (double)J.nx) {
+            lo = min(lo, i);
+            hi = max(hi, i);
+        }
     }
+    atomicMin(&s_lo, lo);   // integer min / max: order independent
+    atomicMax(&s_hi, hi);
+    __syncthreads();
+    if (threadIdx.x == 0) rows_valid[b * WAKE_MAX_REGIONS + r] = make_int2(s_lo, s_hi + 1);
 }
 
 // Resolve one axis from an integer base and an FP32 offset with the
@@ -213,29 +250,28 @@ __device__ __forceinline__ float lerp1(float a, float b, float w) { return fmaf(
 
 // Trilinear FP32 gather of the five fields from ring32 [slot][nx][nz][8]
 // (cell: den, dx_hi, dz, vx | vxx, dx_lo, 0, 0), interpolating t, then x,
-// then z like the reference; density_x in float-float.
-__device__ __forceinline__ Fields5 gather5(const float *__restrict__ ring, int nx, int nz, int s0, int s1,
-                                           float td, int x0, int x1, float xd, int z0, int z1, float zd) {
-    const size_t nxz = (size_t)nx * nz;
-    const size_t dz8 = (size_t)(z1 - z0) * 8;
-    const float4 *p00 = reinterpret_cast<const float4 *>(ring + ((size_t)s0 * nxz + (size_t)x0 * nz + z0) * 8);
-    const float4 *q00 = reinterpret_cast<const float4 *>(ring + ((size_t)s1 * nxz + (size_t)x0 * nz + z0) * 8);
-    const float4 *p10 = reinterpret_cast<const float4 *>(ring + ((size_t)s0 * nxz + (size_t)x1 * nz + z0) * 8);
-    const float4 *q10 = reinterpret_cast<const float4 *>(ring + ((size_t)s1 * nxz + (size_t)x1 * nz + z0) * 8);
-    const size_t dz4 = dz8 / 4;
-    // corner order: [x][z][t]
-    const float4 A0 = __ldg(p00), a0 = __ldg(p00 + 1), A1 = __ldg(p00 + dz4), a1 = __ldg(p00 + dz4 + 1);
-    const float4 B0 = __ldg(q00), b0 = __ldg(q00 + 1), B1 = __ldg(q00 + dz4), b1 = __ldg(q00 + dz4 + 1);
-    const float4 C0 = __ldg(p10), c0 = __ldg(p10 + 1), C1 = __ldg(p10 + dz4), c1 = __ldg(p10 + dz4 + 1);
-    const float4 D0 = __ldg(q10), d0 = __ldg(q10 + 1), D1 = __ldg(q10 + dz4), d1 = __ldg(q10 + dz4 + 1);
+// then z like the reference; density_x in float-float when FF.
+// c<x><t>: float4 index of the z0 cell at x0/x1, t0/t1; dzc: float4 step to z1.
+template <bool FF>
+__device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint32_t c00, uint32_t c01,
+                                           uint32_t c10, uint32_t c11, uint32_t dzc, float td, float xd,
+                                           float zd) {
+    const float4 A0 = __ldg(ring + c00), a0 = __ldg(ring + c00 + 1);
+    const float4 A1 = __ldg(ring + c00 + dzc), a1 = __ldg(ring + c00 + dzc + 1);
+    const float4 B0 = __ldg(ring + c01), b0 = __ldg(ring + c01 + 1);
+    const float4 B1 = __ldg(ring + c01 + dzc), b1 = __ldg(ring + c01 + dzc + 1);
+    const float4 C0 = __ldg(ring + c10), c0 = __ldg(ring + c10 + 1);
+    const float4 C1 = __ldg(ring + c10 + dzc), c1 = __ldg(ring + c10 + dzc + 1);
+    const float4 D0 = __ldg(ring + c11), d0 = __ldg(ring + c11 + 1);
+    const float4 D1 = __ldg(ring + c11 + dzc), d1 = __ldg(ring + c11 + dzc + 1);
     auto tri = [&](float v00a, float v00b, float v01a, float v01b, float v10a, float v10b,
                    float v11a, float v11b) -> float {
-        const float c00 = lerp1(v00a, v00b, td);
-        const float c01 = lerp1(v01a, v01b, td);
-        const float c10 = lerp1(v10a, v10b, td);
-        const float c11 = lerp1(v11a, v11b, td);
-        const float e0 = lerp1(c00, c10, xd);
-        const float e1 = lerp1(c01, c11, xd);
+        const float c00_ = lerp1(v00a, v00b, td);
+        const float c01_ = lerp1(v01a, v01b, td);
+        const float c10_ = lerp1(v10a, v10b, td);
+        const float c11_ = lerp1(v11a, v11b, td);
+        const float e0 = lerp1(c00_, c10_, xd);
+        const float e1 = lerp1(c01_, c11_, xd);
         return lerp1(e0, e1, zd);
     };
     Fields5 r;
@@ -243,15 +279,18 @@ __device__ __forceinline__ Fields5 gather5(const float *__restrict__ ring, int n
     r.dz = tri(A0.z, B0.z, A1.z, B1.z, C0.z, D0.z, C1.z, D1.z);
     r.vx = tri(A0.w, B0.w, A1.w, B1.w, C0.w, D0.w, C1.w, D1.w);
     r.vxx = tri(a0.x, b0.x, a1.x, b1.x, c0.x, d0.x, c1.x, d1.x);
-    {
-        const float2 c00 = lerp_ff(make_float2(A0.y, a0.y), make_float2(B0.y, b0.y), td);
-        const float2 c01 = lerp_ff(make_float2(A1.y, a1.y), make_float2(B1.y, b1.y), td);
-        const float2 c10 = lerp_ff(make_float2(C0.y, c0.y), make_float2(D0.y, d0.y), td);
-        const float2 c11 = lerp_ff(make_float2(C1.y, c1.y), make_float2(D1.y, d1.y), td);
-        const float2 e0 = lerp_ff(c00, c10, xd);
-        const float2 e1 = lerp_ff(c01, c11, xd);
+    if (FF) {
+        const float2 c00_ = lerp_ff(make_float2(A0.y, a0.y), make_float2(B0.y, b0.y), td);
+        const float2 c01_ = lerp_ff(make_float2(A1.y, a1.y), make_float2(B1.y, b1.y), td);
+        const float2 c10_ = lerp_ff(make_float2(C0.y, c0.y), make_float2(D0.y, d0.y), td);
+        const float2 c11_ = lerp_ff(make_float2(C1.y, c1.y), make_float2(D1.y, d1.y), td);
+        const float2 e0 = lerp_ff(c00_, c10_, xd);
+        const float2 e1 = lerp_ff(c01_, c11_, xd);
         const float2 f = lerp_ff(e0, e1, zd);
         r.dx = __fadd_rn(f.x, f.y);
+    } else {
+        r.dx = tri(A0.y + a0.y, B0.y + b0.y, A1.y + a1.y, B1.y + b1.y, C0.y + c0.y, D0.y + d0.y,
+                   C1.y + c1.y, D1.y + d1.y);
     }
     return r;
 }
@@ -264,19 +303,90 @@ __device__ __forceinline__ void kahan(float &s, float &c, float v) {
 }
 
 struct IntegralSmem {
-    float col[C_NF][MX_CHUNK];
-    float row[R_NF][MX_MAX_ROWS];
+    float4 col[MX_CHUNK * CW / 4];
+    float4 row[MX_MAX_ROWS * RW / 4];
     double red[MX_THREADS / 32];
     long long pt;
 };
+
+struct RingView {
+    const float4 *ring;
+    int nt, nx, nz, head, cap;
+    float inv_dt, inv_dz;
+};
+
+// Integrand contribution of rows [i_lo, i_hi) x columns [0, C) of a chunk.
+template <bool FF>
+__device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const RingView &V, int i_lo,
+                                             int i_hi, int C, float &sz, float &cz, float &sx,
+                                             float &cx) {
+    const int total = (i_hi - i_lo) * C;
+    const int tid = threadIdx.x;
+    // (i, jl) of p = tid + k * MX_THREADS, advanced without integer division
+    int i = tid / C, jl = tid - (tid / C) * C;
+    const int di = MX_THREADS / C, dj = MX_THREADS - (MX_THREADS / C) * C;
+    const uint32_t nzc = (uint32_t)V.nz * 2u;   // float4 per x row of a slot
+    for (int p = tid; p < total; p += MX_THREADS) {
+        const float4 *cr = sm.col + jl * (CW / 4);
+        const float4 *rr = sm.row + (i_lo + i) * (RW / 4);
+        const float4 q0 = cr[0], q5 = cr[5];
+        const float4 ra = rr[0];
+        const float wx = rr[1].x;
+        const float ws = q5.w;
+        i += di;
+        jl += dj;
+        if (jl >= C) { jl -= C; i += 1; }
+        if (ws == 0.f || wx == 0.f) continue;
+        const float4 g1 = cr[1];
+        const float u = ra.z;
+        const float r0 = g1.x;
+        const float Dd = u * ((g1.z + 1.f) * u - 2.f * g1.y);
+        const float rad = fmaf(r0, r0, Dd);
+        const float delta = __fdividef(Dd, r0 + rad * rsqrtf(rad));
+        int t0, t1, x0, x1, z0, z1;
+        float td, xd, zd;
+        if (!axis_split(__float_as_int(q0.x), q0.z - delta * V.inv_dt, V.nt, t0, t1, td) ||
+            !axis_split(__float_as_int(ra.x), ra.y, V.nx, x0, x1, xd) ||
+            !axis_split(__float_as_int(q0.y), q0.w + delta * V.inv_dz, V.nz, z0, z1, zd))
+            continue;   // every field is zero outside the history grid
+        int s0 = V.head + t0, s1 = V.head + t1;
+        if (s0 >= V.cap) s0 -= V.cap;
+        if (s1 >= V.cap) s1 -= V.cap;
+        const uint32_t c0x0 = ((uint32_t)s0 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
+        const uint32_t c1x0 = ((uint32_t)s1 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
+        const uint32_t dxc = (uint32_t)(x1 - x0) * nzc;
+        const Fields5 F = gather5<FF>(V.ring, c0x0, c1x0, c0x0 + dxc, c1x0 + dxc,
+                                      2u * (uint32_t)(z1 - z0), td, xd, zd);
+        const float4 q2 = cr[2], q3 = cr[3], q4 = cr[4];
+        const float inv_r = __fdividef(1.f, r0 + delta);
+        const float scale = fmaf(ra.w, g1.w, 1.f);
+        const float vr = F.vx;
+        // brx = (K0x - vx') - vx' (K1x - 1 + vx' K2x); brz = K0z - vx' (K1z + vx' K2z)
+        const float brx = (q3.y - vr) - vr * fmaf(vr, q3.w, q3.z);
+        const float brz = q4.x - vr * fmaf(vr, q4.z, q4.y);
+        const float p1 = fmaf(vr, q2.y, q2.x);
+        const float num = scale * F.dx * brx + F.dz * brz - scale * p1 * F.den * F.vxx;
+        const float Iz = num * inv_r;
+        const float Q1 = q5.x;
+        const float q1 = q4.w - u * Q1;
+        const float M = q5.z - u * Q1 - q5.y * delta;
+        const float e = q2.z;
+        const float pd = -(F.dx * fmaf(vr, q2.w, e) + F.dz * __fdividef(fmaf(vr, e, q3.x), scale)) -
+                         F.den * F.vxx;
+        const float Ix = scale * inv_r * inv_r * (q1 * inv_r * F.den + pd * M);
+        const float w = wx * ws;
+        kahan(sz, cz, w * Iz);
+        kahan(sx, cx, w * Ix);
+    }
+}
 
 // Persistent: CTAs take points of the batch from a work counter.  Writes the
 // FP64 region sums part[b][r][2].
 __global__ void __launch_bounds__(MX_THREADS, 3)
 mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
                int64_t first, int64_t count, size_t rec_words, const float *__restrict__ rec,
-               const PointMeta *__restrict__ meta, double *__restrict__ part,
-               unsigned long long *__restrict__ counter) {
+               const PointMeta *__restrict__ meta, const int2 *__restrict__ rows_valid,
+               double *__restrict__ part, unsigned long long *__restrict__ counter) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     IntegralSmem &sm = *reinterpret_cast<IntegralSmem *>(smem_raw);
     const int tid = threadIdx.x;
@@ -288,72 +398,33 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         const dfcsr_wake_job &J = jobs[job_of_point ? job_of_point[first + b] : 0];
         const PointMeta m = meta[b];
         const float *base = rec + (size_t)b * rec_words;
-        const float inv_dt = (float)(1.0 / J.t_delta), inv_dz = (float)(1.0 / J.z_delta);
-        const float *ring = J.ring32;
-        const int nt = J.nt, nx = J.nx, nz = J.nz, head = J.head, cap = J.cap;
+        RingView V;
+        V.ring = reinterpret_cast<const float4 *>(J.ring32);
+        V.nt = J.nt; V.nx = J.nx; V.nz = J.nz; V.head = J.head; V.cap = J.cap;
+        V.inv_dt = (float)(1.0 / J.t_delta);
+        V.inv_dz = (float)(1.0 / J.z_delta);
         for (int r = 0; r < m.nreg && m.valid; ++r) {
             const RegionMeta R = m.reg[r];
-            const float *rb = base + R.row_off;
-            for (int k = tid; k < R.nxp * R_NF; k += blockDim.x) {
-                const int f = k / R.nxp, i = k - f * R.nxp;
-                sm.row[f][i] = rb[k];
-            }
+            const int2 rv = rows_valid[b * WAKE_MAX_REGIONS + r];
             double reg_z = 0.0, reg_x = 0.0;
-            for (int j0 = 0; j0 < R.nsp; j0 += MX_CHUNK) {
-                const int C = min(MX_CHUNK, R.nsp - j0);
-                const float *cb = base + R.col_off;
-                for (int k = tid; k < C_NF * C; k += blockDim.x) {
-                    const int f = k / C, jl = k - f * C;
-                    sm.col[f][jl] = cb[(size_t)f * R.nsp + j0 + jl];
+            if (rv.y > rv.x) {
+                const float4 *rb = reinterpret_cast<const float4 *>(base + R.row_off);
+                for (int k = tid; k < R.nxp * (RW / 4); k += blockDim.x) sm.row[k] = rb[k];
+                for (int j0 = 0; j0 < R.nsp; j0 += MX_CHUNK) {
+                    const int C = min(MX_CHUNK, R.nsp - j0);
+                    const float4 *cb = reinterpret_cast<const float4 *>(base + R.col_off) + (size_t)j0 * (CW / 4);
+                    for (int k = tid; k < C * (CW / 4); k += blockDim.x) sm.col[k] = cb[k];
+                    __syncthreads();
+                    float sz = 0.f, cz = 0.f, sx = 0.f, cx = 0.f;
+                    if (r == 0)
+                        chunk_points<true>(sm, V, rv.x, rv.y, C, sz, cz, sx, cx);
+                    else
+                        chunk_points<false>(sm, V, rv.x, rv.y, C, sz, cz, sx, cx);
+                    const double bz = block_sum((double)sz - (double)cz, sm.red);
+                    const double bx = block_sum((double)sx - (double)cx, sm.red);
+                    if (tid == 0) { reg_z += bz; reg_x += bx; }
+                    __syncthreads();
                 }
-                __syncthreads();
-                float sz = 0.f, cz = 0.f, sx = 0.f, cx = 0.f;
-                const int total = R.nxp * C;
-                for (int p = tid; p < total; p += blockDim.x) {
-                    const int i = p / C, jl = p - i * C;
-                    const float ws = sm.col[C_WS][jl];
-                    if (ws == 0.f) continue;
-                    const float w = sm.row[R_WX][i] * ws;
-                    const float u = sm.row[R_U][i];
-                    const float r0 = sm.col[C_R0][jl];
-                    const float Dd = u * (sm.col[C_CG][jl] * u - 2.f * sm.col[C_BG][jl]);
-                    const float delta = Dd / (r0 + sqrtf(fmaf(r0, r0, Dd)));
-                    const float rr = r0 + delta;
-                    int t0, t1, x0, x1, z0, z1;
-                    float td, xd, zd;
-                    Fields5 F = {0.f, 0.f, 0.f, 0.f, 0.f};
-                    if (axis_split(__float_as_int(sm.col[C_TB][jl]), sm.col[C_TF][jl] - delta * inv_dt, nt, t0, t1, td) &&
-                        axis_split(__float_as_int(sm.row[R_XB][i]), sm.row[R_XF][i], nx, x0, x1, xd) &&
-                        axis_split(__float_as_int(sm.col[C_ZB][jl]), sm.col[C_ZF][jl] + delta * inv_dz, nz, z0, z1, zd)) {
-                        int s0 = head + t0, s1 = head + t1;
-                        if (s0 >= cap) s0 -= cap;
-                        if (s1 >= cap) s1 -= cap;
-                        F = gather5(ring, nx, nz, s0, s1, td, x0, x1, xd, z0, z1, zd);
-                    }
-                    const float scale = 1.f + sm.row[R_XP][i] * sm.col[C_RHO][jl];
-                    const float vr = F.vx;
-                    // K1x ~ 1 is stored as K1x - 1 so that K0x - vx' (nearly equal
-                    // transverse velocities) is formed exactly
-                    const float brx = (sm.col[C_K0X][jl] - vr) - vr * (sm.col[C_K1X][jl] + vr * sm.col[C_K2X][jl]);
-                    const float brz = sm.col[C_K0Z][jl] - vr * (sm.col[C_K1Z][jl] + vr * sm.col[C_K2Z][jl]);
-                    const float p1 = sm.col[C_A][jl] + vr * sm.col[C_B][jl];
-                    const float num = scale * F.dx * brx + F.dz * brz - scale * p1 * F.den * F.vxx;
-                    const float inv_r = 1.f / rr;
-                    const float Iz = num * inv_r;
-                    const float Q1 = sm.col[C_Q1][jl];
-                    const float q1 = sm.col[C_Q0][jl] - u * Q1;
-                    const float M = sm.col[C_M0][jl] - u * Q1 - sm.col[C_Q2][jl] * delta;
-                    const float e = sm.col[C_E][jl];
-                    const float pd = -(F.dx * (e + vr * sm.col[C_G][jl]) +
-                                       F.dz / scale * (sm.col[C_H][jl] + vr * e)) - F.den * F.vxx;
-                    const float Ix = scale * inv_r * inv_r * (q1 * inv_r * F.den + pd * M);
-                    kahan(sz, cz, w * Iz);
-                    kahan(sx, cx, w * Ix);
-                }
-                const double bz = block_sum((double)sz - (double)cz, sm.red);
-                const double bx = block_sum((double)sx - (double)cx, sm.red);
-                if (tid == 0) { reg_z += bz; reg_x += bx; }
-                __syncthreads();
             }
             if (tid == 0) {
                 part[((size_t)b * WAKE_MAX_REGIONS + r) * 2 + 0] = reg_z;
@@ -389,22 +460,20 @@ mixed_band(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ 
             Region reg[WAKE_MAX_REGIONS];
             wake_regions(J, o.s, o.x, reg);
             const Region R = reg[r];
+            const Axis ax_s = make_axis(R.sl, R.sr, R.nsp);
+            const Axis ax_x = make_axis(R.xl, R.xr, R.nxp);
             for (int j = threadIdx.x; j < R.nsp; j += blockDim.x) {
-                const double spj = np_linspace_at(R.sl, R.sr, R.nsp, j);
+                const double spj = ax_s.at(j);   // same s' as the geometry kernel
                 if (!(fabs(spj - o.s) < J.near_band)) continue;
-                const double dl = (j > 0) ? spj - np_linspace_at(R.sl, R.sr, R.nsp, j - 1) : 0.0;
-                const double dr = (j < R.nsp - 1) ? np_linspace_at(R.sl, R.sr, R.nsp, j + 1) - spj : 0.0;
-                const double ws = 0.5 * (dl + dr);
+                const double ws = ax_s.weight(j);
                 double L[6];
                 lattice_lerp(J, spj, L);
                 const double rho_sp = rho_at(J, spj);
                 for (int i = 0; i < R.nxp; ++i) {
-                    const double xpi = np_linspace_at(R.xl, R.xr, R.nxp, i);
-                    const double xl = (i > 0) ? xpi - np_linspace_at(R.xl, R.xr, R.nxp, i - 1) : 0.0;
-                    const double xr = (i < R.nxp - 1) ? np_linspace_at(R.xl, R.xr, R.nxp, i + 1) - xpi : 0.0;
+                    const double xpi = ax_x.at(i);
                     double Iz, Ix;
                     integrand_fp64(J, o, L, rho_sp, spj, xpi, Iz, Ix);
-                    const double w = 0.5 * (xl + xr) * ws;
+                    const double w = ax_x.weight(i) * ws;
                     az += w * Iz;
                     ax += w * Ix;
                 }
@@ -456,7 +525,9 @@ static const size_t kMixedScratchTarget = (size_t)96 << 20;   // keep batches L2
 static MixedLayout mixed_layout(int xbins_max, int zbins_max, int64_t n) {
     MixedLayout L;
     L.rec_words = point_record_words(xbins_max, zbins_max);
-    int64_t per = (int64_t)(L.rec_words * sizeof(float) + sizeof(PointMeta) + 2 * 8 * WAKE_MAX_REGIONS * 8 + 8 + 64);
+    const int64_t per = (int64_t)(L.rec_words * sizeof(float) + sizeof(PointMeta) +
+                                  2 * 2 * WAKE_MAX_REGIONS * sizeof(double) +
+                                  WAKE_MAX_REGIONS * sizeof(int2) + sizeof(double) + 64);
     int64_t batch = (int64_t)(kMixedScratchTarget / per);
     if (batch < 1) batch = 1;
     if (batch > n) batch = n;
@@ -465,10 +536,12 @@ static MixedLayout mixed_layout(int xbins_max, int zbins_max, int64_t n) {
 }
 
 static size_t mixed_carve(Carver &c, const MixedLayout &L, unsigned long long **counter, float **rec,
-                          PointMeta **meta, double **part, double **band, double **obs_vx) {
+                          PointMeta **meta, int2 **rows, double **part, double **band,
+                          double **obs_vx) {
     *counter = c.take<unsigned long long>(4);
     *rec = c.take<float>((size_t)L.batch * L.rec_words);
     *meta = c.take<PointMeta>((size_t)L.batch);
+    *rows = c.take<int2>((size_t)L.batch * WAKE_MAX_REGIONS);
     *part = c.take<double>((size_t)L.batch * WAKE_MAX_REGIONS * 2);
     *band = c.take<double>((size_t)L.batch * WAKE_MAX_REGIONS * 2);
     *obs_vx = c.take<double>((size_t)L.batch);
@@ -497,8 +570,9 @@ extern "C" size_t dfcsr_wake_workspace_bytes(int xbins_max, int zbins_max, int64
     unsigned long long *a;
     float *b;
     PointMeta *m;
+    int2 *rw;
     double *p, *q, *v;
-    return mixed_carve(c, L, &a, &b, &m, &p, &q, &v) + 256;
+    return mixed_carve(c, L, &a, &b, &m, &rw, &p, &q, &v) + 256;
 }
 
 extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
@@ -518,8 +592,9 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
     unsigned long long *counter;
     float *rec;
     PointMeta *meta;
+    int2 *rows;
     double *part, *band, *obs_vx;
-    mixed_carve(c, L, &counter, &rec, &meta, &part, &band, &obs_vx);
+    mixed_carve(c, L, &counter, &rec, &meta, &rows, &part, &band, &obs_vx);
     if (!workspace || !c.ok()) {
         set_error("dfcsr_wake_mixed: workspace too small (%zu < %zu)", workspace_bytes, c.used);
         return DFCSR_OOM;
@@ -538,13 +613,13 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
         {
             ScopedTiming tm("wake_mixed_geometry", st);
             mixed_geometry<<<dim3((unsigned)count, WAKE_MAX_REGIONS), GEO_THREADS, 0, st>>>(
-                jobs, job_of_point, s, x, first, count, L.rec_words, rec, meta, obs_vx);
+                jobs, job_of_point, s, x, first, count, L.rec_words, rec, meta, rows, obs_vx);
         }
         const int blocks = (int)((int64_t)blocks_max < count ? blocks_max : count);
         {
             ScopedTiming tm("wake_mixed_integral", st);
             mixed_integral<<<blocks, MX_THREADS, sizeof(IntegralSmem), st>>>(
-                jobs, job_of_point, first, count, L.rec_words, rec, meta, part, counter);
+                jobs, job_of_point, first, count, L.rec_words, rec, meta, rows, part, counter);
         }
         if (use_band) {
             ScopedTiming tm("wake_mixed_band", st);

@@ -228,13 +228,19 @@ class DF_tracker:
     def _workspace(self):
         return self.ws or default_workspace()
 
-    def get_DF(self, x, z, px, t, stream=None):
-        """Deposit and finalise the current DF (deposit.py:145-245)."""
+    def get_DF(self, x, z, px, t, stream=None, moments=None):
+        """Deposit and finalise the current DF (deposit.py:145-245).
+
+        ``moments`` (extension): the host copy of ``beam_moments(x, z)`` when
+        the caller already has it for these exact arrays (saves a pass and a
+        device synchronisation)."""
         require_cuda()
         xd, zd, pxd = (as_device_f64(a).reshape(-1) for a in (x, z, px))
         ws = self._workspace()
-        mom = beam_moments(xd, zd, stream, ws)
-        st = mom.cpu().numpy()
+        if moments is None:
+            st = beam_moments(xd, zd, stream, ws).cpu().numpy()
+        else:
+            st = np.asarray(moments, dtype=np.float64)
         self.stats = st
         sigma_x, sigma_z = float(st[3]), float(st[4])
         self.sigma_x, self.sigma_z = sigma_x, sigma_z
