@@ -69,7 +69,8 @@ def jobs_to_device(jobs, device=None):
     """Copy a list of WakeJob structs into one device buffer."""
     raw = b"".join(bytes(j) for j in jobs)
     host = torch.frombuffer(bytearray(raw), dtype=torch.uint8)
-    return host.to(device or torch.device("cuda", torch.cuda.current_device()))
+    return host.pin_memory().to(device or torch.device("cuda", torch.cuda.current_device()),
+                                non_blocking=True)
 
 
 class WakeEvaluator:

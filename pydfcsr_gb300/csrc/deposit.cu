@@ -255,9 +255,39 @@ __global__ void cell_ranges(const uint32_t *__restrict__ keys, int64_t n,
     if (i == n - 1 || keys[i + 1] != k) cend[k] = (uint32_t)(i + 1);
 }
 
-// One warp per lower cell: eight partial sums (corners 00, 01, 10, 11 for
-// channel 0 then channel 1), lanes stride through the cell's particles in
-// sorted (= original) order, then a fixed xor-shuffle tree.
+// Eight partial sums per lower cell (corners 00, 01, 10, 11 for channel 0
+// then channel 1), particles taken in sorted (= original) order.  A warp owns
+// 32 consecutive cells: a cell with at most CELL_SMALL particles is summed by
+// its own lane sequentially; larger cells are then summed by the whole warp
+// (lanes stride through the cell, fixed xor-shuffle tree).  Either way the
+// order of additions is fixed, so the result is deterministic; the split
+// avoids the FP64 shuffle tree (slow on this part) for the many small cells.
+constexpr uint32_t CELL_SMALL = 24;
+
+__device__ __forceinline__ void cell_accumulate(uint32_t idx, int i1, int i2,
+                                                const double *__restrict__ q1, const double *__restrict__ q2,
+                                                const double *__restrict__ w0, const double *__restrict__ w1,
+                                                double start1, double inv1, double start2, double inv2,
+                                                double acc[8]) {
+    const double c1 = __dmul_rn(__dsub_rn(q1[idx], start1), inv1);
+    const double c2 = __dmul_rn(__dsub_rn(q2[idx], start2), inv2);
+    const double s1 = __dsub_rn(1.0, __dsub_rn(c1, (double)i1));
+    const double s2 = __dsub_rn(1.0, __dsub_rn(c2, (double)i2));
+    const double t1 = __dsub_rn(1.0, s1), t2 = __dsub_rn(1.0, s2);
+    const double wa = w0 ? w0[idx] : 1.0;
+    acc[0] = __dadd_rn(acc[0], __dmul_rn(__dmul_rn(wa, s1), s2));
+    acc[1] = __dadd_rn(acc[1], __dmul_rn(__dmul_rn(wa, s1), t2));
+    acc[2] = __dadd_rn(acc[2], __dmul_rn(__dmul_rn(wa, t1), s2));
+    acc[3] = __dadd_rn(acc[3], __dmul_rn(__dmul_rn(wa, t1), t2));
+    if (w1) {
+        const double wb = w1[idx];
+        acc[4] = __dadd_rn(acc[4], __dmul_rn(__dmul_rn(wb, s1), s2));
+        acc[5] = __dadd_rn(acc[5], __dmul_rn(__dmul_rn(wb, s1), t2));
+        acc[6] = __dadd_rn(acc[6], __dmul_rn(__dmul_rn(wb, t1), s2));
+        acc[7] = __dadd_rn(acc[7], __dmul_rn(__dmul_rn(wb, t1), t2));
+    }
+}
+
 __global__ void __launch_bounds__(256)
 cell_sums(const uint32_t *__restrict__ vals, const uint32_t *__restrict__ cstart,
           const uint32_t *__restrict__ cend, uint32_t nkeys, int nb2,
@@ -265,37 +295,42 @@ cell_sums(const uint32_t *__restrict__ vals, const uint32_t *__restrict__ cstart
           const double *__restrict__ w0, const double *__restrict__ w1,
           double start1, double inv1, double start2, double inv2,
           double *__restrict__ partial) {
-    const uint32_t key = (uint32_t)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const uint32_t warp = (uint32_t)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
-    if (key >= nkeys) return;
-    const int i1 = (int)(key / (uint32_t)(nb2 + 1)) - 1;
-    const int i2 = (int)(key % (uint32_t)(nb2 + 1)) - 1;
-    const uint32_t b = cstart[key], e = cend[key];
-    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (uint32_t p = b + lane; p < e; p += 32) {
-        const uint32_t idx = vals[p];
-        const double c1 = __dmul_rn(__dsub_rn(q1[idx], start1), inv1);
-        const double c2 = __dmul_rn(__dsub_rn(q2[idx], start2), inv2);
-        const double s1 = __dsub_rn(1.0, __dsub_rn(c1, (double)i1));
-        const double s2 = __dsub_rn(1.0, __dsub_rn(c2, (double)i2));
-        const double t1 = __dsub_rn(1.0, s1), t2 = __dsub_rn(1.0, s2);
-        const double wa = w0 ? w0[idx] : 1.0;
-        acc[0] = __dadd_rn(acc[0], __dmul_rn(__dmul_rn(wa, s1), s2));
-        acc[1] = __dadd_rn(acc[1], __dmul_rn(__dmul_rn(wa, s1), t2));
-        acc[2] = __dadd_rn(acc[2], __dmul_rn(__dmul_rn(wa, t1), s2));
-        acc[3] = __dadd_rn(acc[3], __dmul_rn(__dmul_rn(wa, t1), t2));
-        if (w1) {
-            const double wb = w1[idx];
-            acc[4] = __dadd_rn(acc[4], __dmul_rn(__dmul_rn(wb, s1), s2));
-            acc[5] = __dadd_rn(acc[5], __dmul_rn(__dmul_rn(wb, s1), t2));
-            acc[6] = __dadd_rn(acc[6], __dmul_rn(__dmul_rn(wb, t1), s2));
-            acc[7] = __dadd_rn(acc[7], __dmul_rn(__dmul_rn(wb, t1), t2));
-        }
+    const uint32_t key0 = warp * 32u;
+    if (key0 >= nkeys) return;
+    const uint32_t key = key0 + (uint32_t)lane;
+    uint32_t b = 0, e = 0;
+    if (key < nkeys) { b = cstart[key]; e = cend[key]; }
+    const bool small = key < nkeys && e - b <= CELL_SMALL;
+    if (small) {
+        double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const int i1 = (int)(key / (uint32_t)(nb2 + 1)) - 1;
+        const int i2 = (int)(key % (uint32_t)(nb2 + 1)) - 1;
+        for (uint32_t p = b; p < e; ++p)
+            cell_accumulate(vals[p], i1, i2, q1, q2, w0, w1, start1, inv1, start2, inv2, acc);
+        double2 *o = reinterpret_cast<double2 *>(partial + (size_t)key * 8);
+        o[0] = make_double2(acc[0], acc[1]);
+        o[1] = make_double2(acc[2], acc[3]);
+        o[2] = make_double2(acc[4], acc[5]);
+        o[3] = make_double2(acc[6], acc[7]);
     }
+    unsigned big = __ballot_sync(0xffffffffu, key < nkeys && !small);
+    while (big) {
+        const int l = __ffs(big) - 1;
+        big &= big - 1;
+        const uint32_t kk = key0 + (uint32_t)l;
+        const uint32_t bb = __shfl_sync(0xffffffffu, b, l), ee = __shfl_sync(0xffffffffu, e, l);
+        const int i1 = (int)(kk / (uint32_t)(nb2 + 1)) - 1;
+        const int i2 = (int)(kk % (uint32_t)(nb2 + 1)) - 1;
+        double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (uint32_t p = bb + lane; p < ee; p += 32)
+            cell_accumulate(vals[p], i1, i2, q1, q2, w0, w1, start1, inv1, start2, inv2, acc);
 #pragma unroll
-    for (int c = 0; c < 8; ++c)
-        for (int o = 16; o > 0; o >>= 1) acc[c] = __dadd_rn(acc[c], __shfl_xor_sync(0xffffffffu, acc[c], o));
-    if (lane < 8) partial[(size_t)key * 8 + lane] = acc[lane];
+        for (int c = 0; c < 8; ++c)
+            for (int o = 16; o > 0; o >>= 1) acc[c] = __dadd_rn(acc[c], __shfl_xor_sync(0xffffffffu, acc[c], o));
+        if (lane < 8) partial[(size_t)kk * 8 + lane] = acc[lane];
+    }
 }
 
 __global__ void cic_assemble(const double *__restrict__ partial, int nb1, int nb2,

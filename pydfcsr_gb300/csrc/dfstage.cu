@@ -13,22 +13,67 @@ namespace dfcsr {
 
 constexpr int SG_TILE = 32;
 constexpr int SG_MAX_WINDOW = 63;
-constexpr int RED_THREADS = 1024;
 
-__global__ void __launch_bounds__(RED_THREADS)
-field_max(const double *__restrict__ f, int n, double *__restrict__ out) {
-    __shared__ double red[32];
-    double m = -INFINITY;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, f[i]);
+// Two-level deterministic reductions: RED_BLOCKS blocks with a fixed
+// element-to-thread assignment, then one block over the partials in order.
+constexpr int RED_BLOCKS = 64;
+
+__device__ __forceinline__ double block_max(double v, double *red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
-    if (lane == 0) red[warp] = m;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) red[warp] = v;
     __syncthreads();
+    double r = v;
     if (threadIdx.x == 0) {
-        double r = red[0];
+        r = red[0];
         for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
-        *out = r;
     }
+    __syncthreads();
+    return r;
+}
+
+// OP 0: max(f); OP 1: sum(g) over f > thr2 and count (thr2 = sc[6] / vth * 8);
+// OP 2: sum(f).  part[b * 2 + {0, 1}].
+template <int OP>
+__global__ void __launch_bounds__(256)
+reduce_partial(const double *__restrict__ f, const double *__restrict__ g, int n,
+               const double *__restrict__ sc, double vth, double *__restrict__ part) {
+    __shared__ double red[8];
+    double a = (OP == 0) ? -INFINITY : 0.0, c = 0.0;
+    double thr2 = 0.0;
+    if (OP == 1) thr2 = __dmul_rn(__ddiv_rn(sc[6], vth), 8.0);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (OP == 0) a = fmax(a, f[i]);
+        else if (OP == 1) { if (f[i] > thr2) { a += g[i]; c += 1.0; } }
+        else a += f[i];
+    }
+    if (OP == 0) {
+        a = block_max(a, red);
+    } else {
+        a = block_sum(a, red);
+        if (OP == 1) c = block_sum(c, red);
+    }
+    if (threadIdx.x == 0) {
+        part[blockIdx.x * 2 + 0] = a;
+        part[blockIdx.x * 2 + 1] = c;
+    }
+}
+
+// Final pass (one warp): OP 0 -> sc[slot] = max; OP 1 -> sc[2] = thr2,
+// sc[3] = sum / count (NaN when empty, like numpy.mean of an empty
+// selection); OP 2 -> sc[slot] = sum / n.
+template <int OP>
+__global__ void reduce_final(const double *__restrict__ part, int nparts, int n, double *__restrict__ sc,
+                             int slot, double vth) {
+    if (threadIdx.x != 0) return;
+    double a = part[0], c = part[1];
+    for (int k = 1; k < nparts; ++k) {
+        if (OP == 0) a = fmax(a, part[2 * k]);
+        else { a += part[2 * k]; c += part[2 * k + 1]; }
+    }
+    if (OP == 0) sc[slot] = a;
+    else if (OP == 1) { sc[2] = __dmul_rn(__ddiv_rn(sc[6], vth), 8.0); sc[3] = a / c; }
+    else sc[slot] = a / (double)n;
 }
 
 // vx[d > thr] /= d[d > thr], thr = max(raw density) / vth  (deposit.py:183-184)
@@ -104,19 +149,30 @@ sg_axis(FieldSet fs, int nx, int nz, int w, const double *__restrict__ coef,
     }
 }
 
-// col[j] = sum_i (dx_i * (d[i+1][j] + d[i][j])) / 2.0 summed row by row
-// (numpy.trapz along axis 0).
-__global__ void trapz_columns(const double *__restrict__ d, int nx, int nz,
-                              const double *__restrict__ dxg, double *__restrict__ col) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nz) return;
+// col[j] = sum_i (dx_i * (d[i+1][j] + d[i][j])) / 2.0 (numpy.trapz along
+// axis 0).  A block covers 32 columns; warp w sums rows w, w + 8, ... of its
+// lane's column in order, then the 8 warp partials are added in order.
+__global__ void __launch_bounds__(256)
+trapz_columns(const double *__restrict__ d, int nx, int nz, const double *__restrict__ dxg,
+              double *__restrict__ col) {
+    __shared__ double part[8][33];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int j = blockIdx.x * 32 + lane;
     double acc = 0.0;
-    for (int i = 0; i < nx - 1; ++i) {
-        const double t = __ddiv_rn(__dmul_rn(dxg[i], __dadd_rn(d[(size_t)(i + 1) * nz + j],
-                                                                d[(size_t)i * nz + j])), 2.0);
-        acc = (i == 0) ? t : __dadd_rn(acc, t);
+    if (j < nz) {
+        for (int i = warp; i < nx - 1; i += 8) {
+            const double t = __ddiv_rn(__dmul_rn(dxg[i], __dadd_rn(d[(size_t)(i + 1) * nz + j],
+                                                                    d[(size_t)i * nz + j])), 2.0);
+            acc = __dadd_rn(acc, t);
+        }
     }
-    col[j] = acc;
+    part[warp][lane] = acc;
+    __syncthreads();
+    if (warp == 0 && j < nz) {
+        double s = part[0][lane];
+        for (int w = 1; w < 8; ++w) s = __dadd_rn(s, part[w][lane]);
+        col[j] = s;
+    }
 }
 
 // dsum = numpy pairwise sum of (dz_j * (col[j+1] + col[j])) / 2.0
@@ -163,37 +219,10 @@ __global__ void gradients(const double *__restrict__ d, const double *__restrict
     vxx_out[t] = grad_at(vx + j, i, nx, (size_t)nz, gx, gxu, gxdx);
 }
 
-// fill = mean(vx_x[density > thr2]) with thr2 = max(density) / vth * 8;
-// count == 0 gives NaN like numpy.mean of an empty selection.
-__global__ void __launch_bounds__(RED_THREADS)
-masked_mean(const double *__restrict__ d, const double *__restrict__ vxx, int n,
-            double *__restrict__ sc, double vth) {
-    __shared__ double red[32];
-    const double thr2 = __dmul_rn(__ddiv_rn(sc[6], vth), 8.0);
-    double s = 0.0, c = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        if (d[i] > thr2) { s += vxx[i]; c += 1.0; }
-    s = block_sum(s, red);
-    c = block_sum(c, red);
-    if (threadIdx.x == 0) {
-        sc[2] = thr2;
-        sc[3] = s / c;
-    }
-}
-
 __global__ void fill_vxx(const double *__restrict__ d, double *__restrict__ vxx, int n,
                          const double *__restrict__ sc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n && d[i] < sc[2]) vxx[i] = sc[3];
-}
-
-__global__ void __launch_bounds__(RED_THREADS)
-field_mean(const double *__restrict__ f, int n, double *__restrict__ out) {
-    __shared__ double red[32];
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s += f[i];
-    s = block_sum(s, red);
-    if (threadIdx.x == 0) *out = s / (double)n;
 }
 
 static int sg_smem_bytes(int w) {
@@ -220,8 +249,9 @@ using namespace dfcsr;
 extern "C" size_t dfcsr_df_workspace_bytes(int nx, int nz) {
     if (nx <= 0 || nz <= 0) return 0;
     const size_t cells = (size_t)nx * nz;
-    // 6 temporary fields, column sums, trapz terms
-    return 6 * align_up(cells * sizeof(double), 256) + 2 * align_up((size_t)nz * sizeof(double), 256) + 512;
+    // 6 temporary fields, column sums, trapz terms, reduction partials
+    return 6 * align_up(cells * sizeof(double), 256) + 2 * align_up((size_t)nz * sizeof(double), 256) +
+           align_up(2 * RED_BLOCKS * sizeof(double), 256) + 512;
 }
 
 extern "C" int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, double *vx,
@@ -254,26 +284,31 @@ extern "C" int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, doub
     double *T0 = c.take<double>(cells), *T1 = c.take<double>(cells), *T2 = c.take<double>(cells);
     double *U0 = c.take<double>(cells), *U1 = c.take<double>(cells), *U2 = c.take<double>(cells);
     double *col = c.take<double>(nz), *terms = c.take<double>(nz);
+    double *rpart = c.take<double>(2 * RED_BLOCKS);
     const int n = (int)cells;
     const int tb = 256, nb = (n + tb - 1) / tb;
     const double vth = p->velocity_threshold;
 
     ScopedTiming tm("df_finalize", s);
-    field_max<<<1, RED_THREADS, 0, s>>>(density, n, sc + 5);
+    reduce_partial<0><<<RED_BLOCKS, 256, 0, s>>>(density, nullptr, n, sc, vth, rpart);
+    reduce_final<0><<<1, 32, 0, s>>>(rpart, RED_BLOCKS, n, sc, 5, vth);
     threshold_divide<<<nb, tb, 0, s>>>(density, vx, n, sc, vth);
     launch_sg(0, FieldSet{{density, vx}, {T0, T1}}, 2, nx, nz, p, s);
     launch_sg(1, FieldSet{{T0, T1}, {density, vx}}, 2, nx, nz, p, s);
-    trapz_columns<<<(nz + 127) / 128, 128, 0, s>>>(density, nx, nz, p->dxg, col);
+    trapz_columns<<<(nz + 31) / 32, 256, 0, s>>>(density, nx, nz, p->dxg, col);
     trapz_final<<<1, 256, 0, s>>>(col, nz, p->dzg, terms, sc);
     normalize_fields<<<nb, tb, 0, s>>>(density, vx, n, sc);
     gradients<<<nb, tb, 0, s>>>(density, vx, nx, nz, p->gx, p->gz, p->gx_uniform, p->gx_dx,
                                 p->gz_uniform, p->gz_dx, U0, U1, U2);
     launch_sg(0, FieldSet{{U0, U1, U2}, {T0, T1, T2}}, 3, nx, nz, p, s);
     launch_sg(1, FieldSet{{T0, T1, T2}, {density_x, density_z, vx_x}}, 3, nx, nz, p, s);
-    field_max<<<1, RED_THREADS, 0, s>>>(density, n, sc + 6);
-    masked_mean<<<1, RED_THREADS, 0, s>>>(density, vx_x, n, sc, vth);
+    reduce_partial<0><<<RED_BLOCKS, 256, 0, s>>>(density, nullptr, n, sc, vth, rpart);
+    reduce_final<0><<<1, 32, 0, s>>>(rpart, RED_BLOCKS, n, sc, 6, vth);
+    reduce_partial<1><<<RED_BLOCKS, 256, 0, s>>>(density, vx_x, n, sc, vth, rpart);
+    reduce_final<1><<<1, 32, 0, s>>>(rpart, RED_BLOCKS, n, sc, 3, vth);
     fill_vxx<<<nb, tb, 0, s>>>(density, vx_x, n, sc);
-    field_mean<<<1, RED_THREADS, 0, s>>>(vx_x, n, sc + 4);
+    reduce_partial<2><<<RED_BLOCKS, 256, 0, s>>>(vx_x, nullptr, n, sc, vth, rpart);
+    reduce_final<2><<<1, 32, 0, s>>>(rpart, RED_BLOCKS, n, sc, 4, vth);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }

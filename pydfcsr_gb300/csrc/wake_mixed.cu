@@ -31,7 +31,7 @@ constexpr int MX_THREADS = 256;
 constexpr int MX_CHUNK = 128;       // s' columns staged in shared memory at once
 constexpr int MX_MAX_ROWS = 1024;   // x' rows per region (2 * xbins)
 constexpr int MX_MAX_COLS = 4096;   // s' columns per region (zbins)
-constexpr int GEO_THREADS = 128;
+constexpr int GEO_THREADS = 256;
 
 // Column record: 28 words (7 float4; stride 112 B keeps 8-lane phases of
 // 16-byte shared loads conflict free).  Row record: 8 words (2 float4).
@@ -100,110 +100,124 @@ __device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *
     if ((size_t)off > rec_words) ok = false;
 }
 
-// grid (points in batch, regions); block GEO_THREADS over columns then rows.
+struct GeoShared {
+    Region reg[WAKE_MAX_REGIONS];
+    RegionMeta rm[WAKE_MAX_REGIONS];
+    double lat_s[6];
+    double vx_obs;
+    int nreg, ok;
+    int lo, hi;
+};
+
+// One CTA per observation point: the per-point constants (regions, orbit at
+// s, vx at the observer) once in thread 0, then every region's s' columns and
+// x' rows across the block.
 __global__ void __launch_bounds__(GEO_THREADS)
 mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
                const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
                size_t rec_words, float *__restrict__ rec, PointMeta *__restrict__ meta,
                int2 *__restrict__ rows_valid, double *__restrict__ obs_vx) {
-    __shared__ int s_lo, s_hi;
+    __shared__ GeoShared gs;
     const int64_t b = blockIdx.x;
     const int64_t pt = first + b;
-    const int r = blockIdx.y;
     if (b >= count) return;
     const dfcsr_wake_job &J = jobs[job_of_point ? job_of_point[pt] : 0];
     const double t = J.position, s = S[pt], x = X[pt];
-    Region reg[WAKE_MAX_REGIONS];
-    const int nreg = wake_regions(J, s, x, reg);
-    RegionMeta rm[WAKE_MAX_REGIONS];
-    bool ok;
-    layout(reg, nreg, rm, ok, rec_words);
-    if (r == 0 && threadIdx.x == 0) {
+    if (threadIdx.x == 0) {
+        gs.nreg = wake_regions(J, s, x, gs.reg);
+        bool ok;
+        layout(gs.reg, gs.nreg, gs.rm, ok, rec_words);
+        gs.ok = ok ? 1 : 0;
         PointMeta m;
-        m.nreg = nreg;
-        m.valid = ok ? 1 : 0;
-        for (int k = 0; k < WAKE_MAX_REGIONS; ++k) m.reg[k] = (k < nreg) ? rm[k] : RegionMeta{0, 0, 0, 0};
+        m.nreg = gs.nreg;
+        m.valid = gs.ok;
+        for (int k = 0; k < WAKE_MAX_REGIONS; ++k)
+            m.reg[k] = (k < gs.nreg) ? gs.rm[k] : RegionMeta{0, 0, 0, 0};
         meta[b] = m;
+        gs.vx_obs = hist_field_fp64(J, 3, t, x, s - t);
+        obs_vx[b] = gs.vx_obs;
+        lattice_lerp(J, s, gs.lat_s);
     }
-    if (!ok || r >= nreg) return;
-    const Region R = reg[r];
-    const double vx_obs = hist_field_fp64(J, 3, t, x, s - t);
-    if (r == 0 && threadIdx.x == 0) obs_vx[b] = vx_obs;
-    double lat_s[6];
-    lattice_lerp(J, s, lat_s);
-    const double X0s = lat_s[0], Y0s = lat_s[1], nsx = lat_s[2], nsy = lat_s[3];
-    const double vxo = lat_s[4] + vx_obs * nsx, vyo = lat_s[5] + vx_obs * nsy;
-    const Axis ax_s = make_axis(R.sl, R.sr, R.nsp);
-    const Axis ax_x = make_axis(R.xl, R.xr, R.nxp);
-    const double xref = ax_x.at(R.nxp / 2);
+    __syncthreads();
+    if (!gs.ok) return;
+    const double X0s = gs.lat_s[0], Y0s = gs.lat_s[1], nsx = gs.lat_s[2], nsy = gs.lat_s[3];
+    const double vxo = gs.lat_s[4] + gs.vx_obs * nsx, vyo = gs.lat_s[5] + gs.vx_obs * nsy;
     const double inv_s = 1.0 / J.s_delta, inv_t = 1.0 / J.t_delta, inv_z = 1.0 / J.z_delta;
     const double inv_x = 1.0 / J.x_delta;
-    float4 *cb = reinterpret_cast<float4 *>(rec + (size_t)b * rec_words + rm[r].col_off);
-    for (int j = threadIdx.x; j < R.nsp; j += blockDim.x) {
-        const double spj = ax_s.at(j);
-        // orbit tables at s' (interpolate1D rule, index by multiplication)
-        double L[6];
-        {
-            int a0, a1;
-            double f;
-            if (axis_index((spj - J.s_min) * inv_s, J.nsample, a0, a1, f)) {
-                const double *pa = J.lattice + (size_t)a0 * 6, *pb = J.lattice + (size_t)a1 * 6;
+    const int nreg = gs.nreg;
+    for (int r = 0; r < nreg; ++r) {
+        const Region R = gs.reg[r];
+        const Axis ax_s = make_axis(R.sl, R.sr, R.nsp);
+        const Axis ax_x = make_axis(R.xl, R.xr, R.nxp);
+        const double xref = ax_x.at(R.nxp / 2);
+        float4 *cb = reinterpret_cast<float4 *>(rec + (size_t)b * rec_words + gs.rm[r].col_off);
+        for (int j = threadIdx.x; j < R.nsp; j += blockDim.x) {
+            const double spj = ax_s.at(j);
+            // orbit tables at s' (interpolate1D rule, index by multiplication)
+            double L[6];
+            {
+                int a0, a1;
+                double f;
+                if (axis_index((spj - J.s_min) * inv_s, J.nsample, a0, a1, f)) {
+                    const double *pa = J.lattice + (size_t)a0 * 6, *pb = J.lattice + (size_t)a1 * 6;
 #pragma unroll
-                for (int k = 0; k < 6; ++k) L[k] = fma(f, pb[k] - pa[k], pa[k]);
-            } else {
+                    for (int k = 0; k < 6; ++k) L[k] = fma(f, pb[k] - pa[k], pa[k]);
+                } else {
 #pragma unroll
-                for (int k = 0; k < 6; ++k) L[k] = 0.0;
+                    for (int k = 0; k < 6; ++k) L[k] = 0.0;
+                }
+            }
+            const double npx = L[2], npy = L[3], tpx = L[4], tpy = L[5];
+            const double Ax = X0s - L[0] + x * nsx, Ay = Y0s - L[1] + x * nsy;
+            const double rx0 = Ax - xref * npx, ry0 = Ay - xref * npy;
+            const double r0 = sqrt(rx0 * rx0 + ry0 * ry0);
+            const double ut0 = (t - r0 - J.t_min) * inv_t;
+            const double uz0 = (spj - (t - r0) - J.z_min) * inv_z;
+            const double tfl = floor(ut0), zfl = floor(uz0);
+            const double a = vxo * tpx + vyo * tpy, bb = vxo * npx + vyo * npy;
+            const double e = tpx * npx + tpy * npy, g = npx * npx + npy * npy;
+            const double h = tpx * tpx + tpy * tpy;
+            const double nmx = nsx - npx, nmy = nsy - npy;
+            const double Q0 = rx0 * nmx + ry0 * nmy;
+            const double q2 = nsx * tpx + nsy * tpy;
+            const bool near = J.near_band > 0.0 && fabs(spj - s) < J.near_band;
+            float4 *o = cb + (size_t)j * (CW / 4);
+            o[0] = make_float4(__int_as_float(clamp_int(tfl)), __int_as_float(clamp_int(zfl)),
+                               (float)(ut0 - tfl), (float)(uz0 - zfl));
+            o[1] = make_float4((float)r0, (float)(rx0 * npx + ry0 * npy), (float)(g - 1.0),
+                               (float)rho_at(J, spj));
+            o[2] = make_float4((float)a, (float)bb, (float)e, (float)g);
+            o[3] = make_float4((float)h, (float)(bb - a * e), (float)((a * g - 1.0) + bb * e),
+                               (float)(bb * g));
+            o[4] = make_float4((float)(a * (1.0 - h)), (float)(a * e + bb * h), (float)(bb * e),
+                               (float)Q0);
+            o[5] = make_float4((float)(npx * nmx + npy * nmy), (float)q2, (float)(Q0 - q2 * r0),
+                               near ? 0.f : (float)ax_s.weight(j));   // band columns: FP64 kernel
+        }
+        // rows: x cell, offset, u = x' - x'_ref, x', trapz weight; valid row range
+        if (threadIdx.x == 0) { gs.lo = R.nxp; gs.hi = -1; }
+        __syncthreads();
+        float4 *rb = reinterpret_cast<float4 *>(rec + (size_t)b * rec_words + gs.rm[r].row_off);
+        const double ux_first = (R.xl - J.x_min) * inv_x, dux = ax_x.step * inv_x;
+        int lo = R.nxp, hi = -1;
+        for (int i = threadIdx.x; i < R.nxp; i += blockDim.x) {
+            const double xpi = ax_x.at(i);
+            const double ux = fma((double)i, dux, ux_first);
+            const double fb = floor(ux);
+            rb[2 * i] = make_float4(__int_as_float(clamp_int(fb)), (float)(ux - fb), (float)(xpi - xref),
+                                    (float)xpi);
+            rb[2 * i + 1] = make_float4((float)ax_x.weight(i), 0.f, 0.f, 0.f);
+            if (ux > -1.0 && ux < (double)J.nx) {
+                lo = min(lo, i);
+                hi = max(hi, i);
             }
         }
-        const double npx = L[2], npy = L[3], tpx = L[4], tpy = L[5];
-        const double Ax = X0s - L[0] + x * nsx, Ay = Y0s - L[1] + x * nsy;
-        const double rx0 = Ax - xref * npx, ry0 = Ay - xref * npy;
-        const double r0 = sqrt(rx0 * rx0 + ry0 * ry0);
-        const double ut0 = (t - r0 - J.t_min) * inv_t;
-        const double uz0 = (spj - (t - r0) - J.z_min) * inv_z;
-        const double tfl = floor(ut0), zfl = floor(uz0);
-        const double a = vxo * tpx + vyo * tpy, bb = vxo * npx + vyo * npy;
-        const double e = tpx * npx + tpy * npy, g = npx * npx + npy * npy;
-        const double h = tpx * tpx + tpy * tpy;
-        const double nmx = nsx - npx, nmy = nsy - npy;
-        const double Q0 = rx0 * nmx + ry0 * nmy;
-        const double q2 = nsx * tpx + nsy * tpy;
-        const bool near = J.near_band > 0.0 && fabs(spj - s) < J.near_band;
-        float4 *o = cb + (size_t)j * (CW / 4);
-        o[0] = make_float4(__int_as_float(clamp_int(tfl)), __int_as_float(clamp_int(zfl)),
-                           (float)(ut0 - tfl), (float)(uz0 - zfl));
-        o[1] = make_float4((float)r0, (float)(rx0 * npx + ry0 * npy), (float)(g - 1.0),
-                           (float)rho_at(J, spj));
-        o[2] = make_float4((float)a, (float)bb, (float)e, (float)g);
-        o[3] = make_float4((float)h, (float)(bb - a * e), (float)((a * g - 1.0) + bb * e),
-                           (float)(bb * g));
-        o[4] = make_float4((float)(a * (1.0 - h)), (float)(a * e + bb * h), (float)(bb * e),
-                           (float)Q0);
-        o[5] = make_float4((float)(npx * nmx + npy * nmy), (float)q2, (float)(Q0 - q2 * r0),
-                           near ? 0.f : (float)ax_s.weight(j));   // band columns: FP64 kernel
+        atomicMin(&gs.lo, lo);   // integer min / max: order independent
+        atomicMax(&gs.hi, hi);
+        __syncthreads();
+        if (threadIdx.x == 0) rows_valid[b * WAKE_MAX_REGIONS + r] = make_int2(gs.lo, gs.hi + 1);
+        __syncthreads();
     }
-    // rows: x cell, offset, u = x' - x'_ref, x', trapz weight; valid row range
-    if (threadIdx.x == 0) { s_lo = R.nxp; s_hi = -1; }
-    __syncthreads();
-    float4 *rb = reinterpret_cast<float4 *>(rec + (size_t)b * rec_words + rm[r].row_off);
-    const double ux_first = (R.xl - J.x_min) * inv_x, dux = ax_x.step * inv_x;
-    int lo = R.nxp, hi = -1;
-    for (int i = threadIdx.x; i < R.nxp; i += blockDim.x) {
-        const double xpi = ax_x.at(i);
-        const double ux = fma((double)i, dux, ux_first);
-        const double fb = floor(ux);
-        rb[2 * i] = make_float4(__int_as_float(clamp_int(fb)), (float)(ux - fb), (float)(xpi - xref),
-                                (float)xpi);
-        rb[2 * i + 1] = make_float4((float)ax_x.weight(i), 0.f, 0.f, 0.f);
-        if (ux > -1.0 && ux < (double)J.nx) {
-            lo = min(lo, i);
-            hi = max(hi, i);
-        }
-    }
-    atomicMin(&s_lo, lo);   // integer min / max: order independent
-    atomicMax(&s_hi, hi);
-    __syncthreads();
-    if (threadIdx.x == 0) rows_valid[b * WAKE_MAX_REGIONS + r] = make_int2(s_lo, s_hi + 1);
 }
 
 // Resolve one axis from an integer base and an FP32 offset with the
@@ -612,7 +626,7 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
         DFCSR_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
         {
             ScopedTiming tm("wake_mixed_geometry", st);
-            mixed_geometry<<<dim3((unsigned)count, WAKE_MAX_REGIONS), GEO_THREADS, 0, st>>>(
+            mixed_geometry<<<(unsigned)count, GEO_THREADS, 0, st>>>(
                 jobs, job_of_point, s, x, first, count, L.rec_words, rec, meta, rows, obs_vx);
         }
         const int blocks = (int)((int64_t)blocks_max < count ? blocks_max : count);

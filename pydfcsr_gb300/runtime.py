@@ -50,13 +50,23 @@ def as_device_f64(a, device=None):
             t = t.to(torch.float64)
         return t.contiguous()
     arr = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
-    return torch.from_numpy(arr).to(dev)
+    return _async_upload(arr, dev)
+
+
+def _async_upload(a, dev):
+    """Stage through torch's caching pinned-host allocator and copy without
+    blocking the host; the allocator keeps the staging block alive until the
+    copy has run on the current stream."""
+    t = torch.from_numpy(a)
+    if t.numel() == 0:
+        return t.to(dev)
+    return t.pin_memory().to(dev, non_blocking=True)
 
 
 def host_to_device(arr, dtype=None, device=None):
     dev = device or torch.device("cuda", torch.cuda.current_device())
     a = np.ascontiguousarray(arr if dtype is None else np.asarray(arr, dtype=dtype))
-    return torch.from_numpy(a).to(dev)
+    return _async_upload(a, dev)
 
 
 class Workspace:
