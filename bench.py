@@ -56,6 +56,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison leg")
+    ap.add_argument("--serve-requests", type=int, default=256,
+                    help="requests in the serving stream (0 skips the serving leg)")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate (1/s)")
+    ap.add_argument("--serve-fp64-sample", type=int, default=6,
+                    help="requests of the stream served by both the mixed and the FP64 kernels")
     return ap.parse_args()
 
 
@@ -349,12 +354,58 @@ def gpu_arm(a):
                       "ms_per_step": e2e_s * 1000 / K}
         del re2e, host_sets
 
+    if a.serve_requests > 0 and a.precision == "mixed":
+        out["serving"] = serving_leg(a.serve_requests, a.serve_rate, a.serve_fp64_sample,
+                                     seed=4 + 1000 * rank)
+
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(wl, lattice, sample_steps=2, warm_steps=4, n_obs=32)
     if world > 1:
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(out))
+
+
+def serving_leg(n_requests, rate_hz, fp64_sample, seed=4):
+    """The request stream (single dipoles, rho ~ U(1, 20) m, angle ~
+    U(0.02, 0.2), N ~ logU(1e5, 4e6), sigma_z ~ U(10, 100) um, grid from
+    {64, 128, 256, 512}^2, mesh side from {32, 64, 96, 128}; 8 DF steps per
+    request and a wake on its mesh at steps 2..8) served with continuous
+    batching; then its first ``fp64_sample`` requests, all arriving at t = 0,
+    served by the mixed and by the plain FP64 kernels for the speed-up and
+    the error on the same requests."""
+    import torch
+    from pydfcsr_gb300.serve import RequestSpec, WakeServer
+    from pydfcsr_gb300.synthetic import serving_requests
+    reqs = serving_requests(n_requests=n_requests, rate_hz=rate_hz, seed=seed)
+    srv = WakeServer(reqs, precision="mixed")
+    full = srv.run()
+    del srv
+    torch.cuda.empty_cache()
+    out = {"stream": f"{n_requests} requests, Poisson arrivals at {rate_hz:g}/s (seed {seed}), "
+                     "8 DF steps + 7 wakes each, 100x100 integration bins",
+           "mixed": full}
+    if fp64_sample > 0:
+        sample = [RequestSpec.from_dict({**r, "arrival_s": 0.0}) for r in reqs[:fp64_sample]]
+        m = WakeServer(sample, precision="mixed")
+        sm = m.run()
+        p = WakeServer(sample, precision="fp64")
+        sp = p.run()
+        worst, rms = 0.0, 0.0
+        for r in sample:
+            for (k, dE1, xk1), (_, dE2, xk2) in zip(m.result(r.id), p.result(r.id)):
+                e = wake_errors(dE1, xk1, dE2, xk2)
+                worst = max(worst, e["max_rel"])
+                rms = max(rms, e["rms_rel"])
+        out["same_requests"] = {"requests": len(sample), "mixed": sm, "fp64": sp,
+                                "mixed_speedup": sm["wake_points_per_s"] / sp["wake_points_per_s"],
+                                "max_rel_vs_fp64": worst, "worst_rms_rel_vs_fp64": rms,
+                                "error_definition": "per request and step, S = peak |wake| over "
+                                "both components of the FP64 result; max_rel = max|a-b|/S, rms_rel "
+                                "= ||a-b||/||b||; worst over all requests and steps"}
+        del m, p
+        torch.cuda.empty_cache()
+    return out
 
 
 def wake_errors(dE, xk, dE_ref, xk_ref):

@@ -50,7 +50,8 @@ size_t dfcsr_abi_sizeof(int which);
  * dfcsr_timing_collect() waits for the recorded events and adds their
  * durations to per-kernel totals, read with dfcsr_timing_get(name, ...).
  * Names: beam_moments, deposit_cic2d, df_finalize, history_regrid,
- * wake_fp64, wake_mixed_geometry, wake_mixed_integral, wake_mixed_band. */
+ * wake_fp64, wake_mixed_geometry, wake_mixed_integral, wake_mixed_band,
+ * transport6, apply_wakes. */
 void dfcsr_timing_enable(int on);
 int dfcsr_timing_collect(void);
 int dfcsr_timing_get(const char *name, double *total_ms, long long *launches);
@@ -242,6 +243,31 @@ int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
                      int xbins_max, int zbins_max, int use_band,
                      double *dE, double *xkick,
                      void *workspace, size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Particle steps on either side of the wake.  `coords` is the beam's
+ * [6, ld] row-major FP64 array (rows x, px, y, py, z, pz; particle i is
+ * column i), updated in place. */
+
+/* Linear transport coords <- R coords by a 6x6 matrix (R: HOST pointer, 36
+ * doubles, row-major; copied into the launch, so it may be reused at once).
+ * No counterpart on the reference's run path: there Beam.track
+ * (beams.py:101-106) calls bmadx's track_element (third party); the linear
+ * matrices come from r_gen6 (r_gen6.py:4-122).  Each output row is a fused
+ * multiply-add chain over the non-zero coefficients in increasing column. */
+int dfcsr_transport6(const double *R, double *coords, int64_t n, int64_t ld, void *stream);
+
+/* Beam.apply_wakes (beams.py:108-131): tables step * wake * 1e6 / energy,
+ * RegularGridInterpolator (linear, fill 0) at (x_transform, z) with
+ * x_transform = x - (slope0 * z + slope1), pz += dE term, and px += x-kick
+ * term when transverse_on.  dE_dct / x_kick: [nx, nz] row-major; xrange
+ * [nx], zrange [nz] ascending.  Scratch: dfcsr_apply_wakes_workspace_bytes. */
+size_t dfcsr_apply_wakes_workspace_bytes(int nx, int nz);
+int dfcsr_apply_wakes(double *coords, int64_t n, int64_t ld, const double *dE_dct,
+                      const double *x_kick, const double *xrange, const double *zrange,
+                      int nx, int nz, double slope0, double slope1, double step_size,
+                      double init_energy, int transverse_on, void *workspace,
+                      size_t workspace_bytes, void *stream);
 
 #ifdef __cplusplus
 }

@@ -22,6 +22,7 @@ DFTracker.build_interp...  deposit.py:395-426
 reference_trajectory       lattice.py:4-110, 136-150
 csr_mesh                   CSR.py:361-394
 WakeOracle.wake / points   CSR.py:397-418, 454-782  (C)
+apply_wakes                beams.py:108-131
 =========================  ==========================================
 
 Third-party arithmetic the reference calls, restated from the published
@@ -62,7 +63,7 @@ _SRC = os.path.join(HERE, "csr_oracle.c")
 
 __all__ = ["build", "histogram_cic_2d", "interpolate3D", "interpolate1D",
            "savgol_filter", "gradient2d", "DFTracker", "reference_trajectory",
-           "csr_mesh", "beam_stats", "WakeOracle"]
+           "csr_mesh", "beam_stats", "WakeOracle", "apply_wakes"]
 
 
 def build(force=False):
@@ -263,6 +264,23 @@ def rgi_linear_2d(xg, zg, values, X, Z, fill_value):
     oob = (X < xg[0]) | (X > xg[-1]) | (Z < zg[0]) | (Z > zg[-1])
     out = np.where(oob, fill_value, out)
     return out
+
+
+def apply_wakes(coords, dE_dct, x_kick, xrange, zrange, step_size, init_energy,
+                transverse_on, slope):
+    """Beam.apply_wakes (beams.py:108-131) on a (6, N) array; returns the
+    kicked copy.  ``slope`` is the polyfit of x on z that the reference's
+    x_transform property computes (beams.py:201-211)."""
+    c = np.array(coords, dtype=float, copy=True)
+    xt = c[0] - np.polyval(slope, c[4])
+    dE_E1 = step_size * np.asarray(dE_dct, float) * 1e6 / init_energy
+    c[5] = c[5] + rgi_linear_2d(np.asarray(xrange, float), np.asarray(zrange, float), dE_E1,
+                                xt, c[4], 0.0)
+    if transverse_on:
+        dxp = step_size * np.asarray(x_kick, float) * 1e6 / init_energy
+        c[1] = c[1] + rgi_linear_2d(np.asarray(xrange, float), np.asarray(zrange, float), dxp,
+                                    xt, c[4], 0.0)
+    return c
 
 
 # ------------------------------------------------------------------ DF_tracker

@@ -105,7 +105,7 @@ class CSR2D:
 
     def __init__(self, input_file=None, parallel=False, *, beam=None, lattice=None,
                  particle_deposition=None, CSR_integration=None, CSR_computation=None,
-                 precision="fp64", grid_rule="reference", near_band=0.0):
+                 precision="fp64", grid_rule="reference", near_band=0.0, workspace=None):
         if input_file is not None:
             raise NotImplementedError(
                 "YAML input files need bmadx/distgen beams; build a Beam and pass beam=, "
@@ -117,12 +117,12 @@ class CSR2D:
         self.beam = beam
         self.lattice = lattice if isinstance(lattice, Lattice) or lattice is None else Lattice(lattice)
         self.DF_tracker = DF_tracker(particle_deposition or {}, precision=precision,
-                                     grid_rule=grid_rule)
+                                     grid_rule=grid_rule, workspace=workspace)
         self.integration_params = Integration_params(CSR_integration or {})
         self.CSR_params = CSR_params(CSR_computation or {})
         self.formation_length = None
         self.parallel = False
-        self.evaluator = WakeEvaluator()
+        self.evaluator = WakeEvaluator(workspace)
         self._jobs_dev = None
         if beam is not None:
             self.initialization()

@@ -18,24 +18,36 @@ __all__ = ["Beam"]
 
 
 class Beam:
-    def __init__(self, coords, charge=1e-9, energy=1e9, position=0.0):
+    def __init__(self, coords, charge=1e-9, energy=1e9, position=0.0, workspace=None,
+                 adopt=False):
         require_cuda()
+        self.ws = workspace
         self._charge = float(charge)
         self._init_energy = float(energy)
         self.position = float(position)
         self.step = 0
-        self.set_coords(coords)
+        self.set_coords(coords, adopt)
 
-    def set_coords(self, coords):
-        """Replace the particle coordinates (array-like [6, N])."""
+    def set_coords(self, coords, adopt=False):
+        """Replace the particle coordinates (array-like [6, N]).
+
+        A CUDA float64 tensor passed in is used as is.  Unless ``adopt`` is
+        true it is copied before the first in-place update (track,
+        apply_wakes), so the caller's tensor keeps its values."""
         c = as_device_f64(coords)
         if c.dim() != 2 or c.shape[0] != 6:
             raise ValueError("coords must have shape (6, N)")
         self.particle = c
+        self._owned = adopt or c is not coords
         self.update_status()
 
+    def _own(self):
+        if not self._owned:
+            self.particle = self.particle.clone()
+            self._owned = True
+
     def update_status(self):
-        m = beam_moments(self.particle[0], self.particle[4])
+        m = beam_moments(self.particle[0], self.particle[4], ws=self.ws)
         self._moments_dev = m
         st = m.cpu().numpy()
         self._moments = st
@@ -43,13 +55,42 @@ class Beam:
         self._sigma_x, self._sigma_z = float(st[3]), float(st[4])
         self._slope = np.array([st[5], st[6]])
 
+    def transport(self, R):
+        """coords <- R coords in place (6x6 FP64 matrix, e.g. from r_gen6)."""
+        self._own()
+        Rh = np.ascontiguousarray(np.asarray(R, dtype=np.float64))
+        if Rh.shape != (6, 6):
+            raise ValueError("R must be 6x6")
+        n = self.particle.shape[1]
+        _lib.call("dfcsr_transport6", Rh.ctypes.data_as(ctypes.c_void_p), ptr(self.particle), n,
+                  self.particle.stride(0), stream_handle())
+
     def track(self, R, step_size, update_step=True):
-        """Apply a 6x6 transfer matrix (e.g. from r_gen6) and advance."""
-        Rt = torch.as_tensor(np.asarray(R, dtype=np.float64), device=self.particle.device)
-        self.particle = (Rt @ self.particle).contiguous()
+        """Apply a 6x6 transfer matrix and advance (beams.py:101-106 with a
+        linear matrix in place of bmadx's track_element)."""
+        self.transport(R)
         self.position += step_size
         if update_step:
             self.step += 1
+        self.update_status()
+
+    def apply_wakes(self, dE_dct, x_kick, xrange, zrange, step_size, transverse_on):
+        """Kick pz (and px when ``transverse_on``) by the wake interpolated at
+        (x_transform, z) (beams.py:108-131); updates the statistics."""
+        self._own()
+        dE = as_device_f64(dE_dct)
+        xk = as_device_f64(x_kick) if transverse_on else None
+        xr, zr = as_device_f64(xrange), as_device_f64(zrange)
+        nx, nz = xr.numel(), zr.numel()
+        if tuple(dE.shape) != (nx, nz) or (xk is not None and tuple(xk.shape) != (nx, nz)):
+            raise ValueError("wake tables must have shape (len(xrange), len(zrange))")
+        ws = (self.ws or default_workspace()).get(
+            "apply_wakes", _lib.query("dfcsr_apply_wakes_workspace_bytes", nx, nz))
+        n = self.particle.shape[1]
+        _lib.call("dfcsr_apply_wakes", ptr(self.particle), n, self.particle.stride(0), ptr(dE),
+                  ptr(xk), ptr(xr), ptr(zr), nx, nz, float(self._slope[0]), float(self._slope[1]),
+                  float(step_size), self._init_energy, 1 if transverse_on else 0, ptr(ws),
+                  ws.numel(), stream_handle())
         self.update_status()
 
     @property

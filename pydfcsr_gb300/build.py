@@ -26,6 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-I", INCLUDE]
 UNITS = {
+    "beam_ops.cu": [],
     "capi.cu": [],
     "deposit.cu": [],
     "deposit_noalloc.cu": [],

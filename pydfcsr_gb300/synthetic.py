@@ -34,7 +34,7 @@ import numpy as np
 
 from .r_gen6 import r_gen6
 
-__all__ = ["Workload", "workload", "gaussian_beam", "double_horn_beam",
+__all__ = ["Workload", "workload", "gaussian_beam", "gaussian_beam_device", "double_horn_beam",
            "dipole_lattice", "chicane_lattice", "StepPlan", "serving_requests"]
 
 C_LIGHT = 299792458.0
@@ -78,6 +78,24 @@ def gaussian_beam(n, sigma_x, sigma_z, sigma_delta=1e-4, sigma_xp=5e-6,
     out[3] = rng.normal(0.0, sigma_xp, n)
     out[4] = rng.normal(0.0, sigma_z, n)
     out[5] = chirp * out[4] + rng.normal(0.0, sigma_delta, n)
+    return out
+
+
+def gaussian_beam_device(n, sigma_x, sigma_z, sigma_delta=1e-4, sigma_xp=5e-6, chirp=0.0,
+                         seed=1, device=None):
+    """``gaussian_beam`` drawn on the GPU from a seeded torch CUDA generator
+    (same layout; not the same numbers as the numpy generator).  Used by the
+    request stream, whose beams are too many to draw on the host."""
+    import torch
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    g = torch.Generator(device=dev)
+    g.manual_seed(int(seed))
+    out = torch.randn((6, n), generator=g, dtype=torch.float64, device=dev)
+    scale = torch.tensor([sigma_x, sigma_xp, sigma_x, sigma_xp, sigma_z, sigma_delta],
+                         dtype=torch.float64).to(dev, non_blocking=True)
+    out.mul_(scale[:, None])
+    if chirp:
+        out[5].add_(out[4], alpha=chirp)
     return out
 
 

@@ -25,6 +25,7 @@ Fixtures:
   wake_*.npz    get_CSR_mesh, get_CSR_wake (with debug integrands) and
                 calculate_2D_CSR for an unchirped dipole and for both signs of
                 chirp (the 4-region branch).
+  apply_wakes.npz  Beam.apply_wakes with and without the transverse kick.
 """
 import os
 import sys
@@ -327,8 +328,38 @@ def gen_wake(R, tag, lattice, beam, n_steps, dep, integ, mesh, points, debug_poi
     save(f"wake_{tag}.npz", **out)
 
 
+def gen_apply_wakes(R):
+    """Beam.apply_wakes (beams.py:108-131) on a chirped beam: a wake table on
+    a 9 x 11 mesh (CSR_xrange_transformed x CSR_zrange), particles inside and
+    outside the mesh, with and without the transverse kick."""
+    import collections
+    import pyDFCSR_2D.beams as B
+    Part = collections.namedtuple("Particle", "x px y py z pz s p0c mc2")
+    B.Particle = Part          # the shim's bmadx stand-in carries no fields
+    coords = gaussian_beam(1500, 20e-6, 50e-6, 1e-4, 5e-6, -10.0, seed=44)
+    coords[0] += 1.1 * coords[4]          # x-z correlation: x_transform != x
+    rng = np.random.default_rng(45)
+    x, z = coords[0], coords[4]
+    p = np.polyfit(z, x, deg=1)
+    xt = x - np.polyval(p, z)
+    xr = np.linspace(xt.mean() - 2.5 * xt.std(), xt.mean() + 2.5 * xt.std(), 9)
+    zr = np.linspace(z.mean() - 2.5 * z.std(), z.mean() + 2.5 * z.std(), 11)
+    dE = rng.normal(0.0, 2.0, (9, 11))
+    xk = rng.normal(0.0, 0.5, (9, 11))
+    out = {"coords": coords, "xrange": xr, "zrange": zr, "dE_dct": dE, "x_kick": xk,
+           "step_size": np.array(0.013), "init_energy": np.array(1e9), "slope": p}
+    for tag, transverse in (("t", True), ("l", False)):
+        b = object.__new__(B.Beam)
+        b.particle = Part(*[coords[k].copy() for k in range(6)], 0.0, 1e9, 0.511e6)
+        b._init_energy = 1e9
+        b.apply_wakes(dE, xk, xr, zr, 0.013, transverse)
+        out[f"out_{tag}"] = np.array([getattr(b.particle, f) for f in ("x", "px", "y", "py", "z", "pz")])
+    save("apply_wakes.npz", **out)
+
+
 def main(ref_root):
     R = ref_shim.install(ref_root)
+    gen_apply_wakes(R)
     gen_interp(R)
     gen_cic(R)
     gen_df(R)

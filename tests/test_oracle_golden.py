@@ -247,3 +247,16 @@ def test_step_plan_positions():
     p = StepPlan(chicane_lattice(0.065))
     assert len(p.positions) == 101
     assert p.positions[-1] == pytest.approx(6.5)
+
+
+def test_apply_wakes_golden():
+    """Beam.apply_wakes: pz (and px with the transverse kick) from the
+    reference on a chirped beam, particles inside and outside the mesh."""
+    g = golden("apply_wakes.npz")
+    args = (g["dE_dct"], g["x_kick"], g["xrange"], g["zrange"], float(g["step_size"]),
+            float(g["init_energy"]))
+    for tag, transverse in (("t", True), ("l", False)):
+        out = O.apply_wakes(g["coords"], *args, transverse, g["slope"])
+        np.testing.assert_array_equal(out, g[f"out_{tag}"])
+    moved = g["out_t"][5] != g["coords"][5]
+    assert 0 < moved.sum() < moved.size      # some particles lie outside the mesh
