@@ -81,8 +81,10 @@ int dfcsr_beam_moments(const double *x, const double *z, int64_t n, double *out,
  *                                                 w1 required when n > 0)
  * Bin spacing (end - start) / nbins, lower bin floor(cell), weights
  * 1 - frac, bounds-checked corners - exactly the reference's rule.
- * Deterministic: particles are sorted by lower cell (stable LSD radix sort)
- * and each cell is summed by one warp in a fixed order.  No float atomics.
+ * Deterministic: particles are sorted by lower cell (stable LSD radix sort);
+ * fixed-size chunks of the sorted particles are summed per cell and the
+ * parts of cells that cross chunks are added in chunk order.  No float
+ * atomics; the order of additions depends only on the input order.
  * Needs dfcsr_deposit_workspace_bytes(n, nb1, nb2) bytes of scratch.
  */
 size_t dfcsr_deposit_workspace_bytes(int64_t n, int nb1, int nb2);

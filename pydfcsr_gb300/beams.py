@@ -5,14 +5,18 @@ scope).  Here the 6D coordinates (x, px, y, py, z, pz) live in one float64
 CUDA tensor [6, N]; the statistics the wake needs (beams.py:137-215: means,
 standard deviations, the polyfit slope of x on z and the chirp-removed
 x_transform) come from one deterministic device moments call per update.
-Linear transport by a 6x6 matrix (``track``) stands in for bmadx on linear
-lattices.
+Linear transport by a 6x6 matrix (``track``, one ``dfcsr_transport6`` launch)
+stands in for bmadx on linear lattices; ``apply_wakes`` is beams.py:108-131 as
+one ``dfcsr_apply_wakes`` call.
 """
+import ctypes
+
 import numpy as np
 import torch
 
+from . import _lib
 from .deposit import beam_moments
-from .runtime import as_device_f64, require_cuda
+from .runtime import as_device_f64, default_workspace, ptr, require_cuda, stream_handle
 
 __all__ = ["Beam"]
 
@@ -38,7 +42,9 @@ class Beam:
         if c.dim() != 2 or c.shape[0] != 6:
             raise ValueError("coords must have shape (6, N)")
         self.particle = c
-        self._owned = adopt or c is not coords
+        shared = (isinstance(coords, torch.Tensor) and coords.is_cuda
+                  and c.untyped_storage().data_ptr() == coords.untyped_storage().data_ptr())
+        self._owned = adopt or not shared
         self.update_status()
 
     def _own(self):

@@ -256,81 +256,121 @@ __global__ void cell_ranges(const uint32_t *__restrict__ keys, int64_t n,
 }
 
 // Eight partial sums per lower cell (corners 00, 01, 10, 11 for channel 0
-// then channel 1), particles taken in sorted (= original) order.  A warp owns
-// 32 consecutive cells: a cell with at most CELL_SMALL particles is summed by
-// its own lane sequentially; larger cells are then summed by the whole warp
-// (lanes stride through the cell, fixed xor-shuffle tree).  Either way the
-// order of additions is fixed, so the result is deterministic; the split
-// avoids the FP64 shuffle tree (slow on this part) for the many small cells.
-constexpr uint32_t CELL_SMALL = 24;
+// then channel 1), deterministic and load-balanced over the sorted particles.
+//
+// seg_sums: thread t takes the SEG_K sorted positions [t*K, t*K + K) (staged
+// through shared memory) and sums each run of equal cell keys in order.  A
+// run whose cell lies wholly inside the chunk is the cell's sum and is
+// written to partial[cell]; a cell that crosses a chunk edge leaves its part
+// of this chunk in chunk_first[t] (the run that starts the chunk) or
+// chunk_last[t] (the run that ends it).
+// seg_combine: one thread per cell adds the chunk parts of crossing cells in
+// chunk order and writes zeros for empty cells.
+// The order of every addition depends only on the sorted order, which the
+// stable sort fixes: the result does not change from run to run.
+constexpr int SEG_K = 16;
+constexpr int SEG_THREADS = 256;
+constexpr int SEG_TILE = SEG_K * SEG_THREADS;
 
-__device__ __forceinline__ void cell_accumulate(uint32_t idx, int i1, int i2,
+__device__ __forceinline__ void cell_accumulate(uint32_t idx, double fi1, double fi2,
                                                 const double *__restrict__ q1, const double *__restrict__ q2,
                                                 const double *__restrict__ w0, const double *__restrict__ w1,
                                                 double start1, double inv1, double start2, double inv2,
                                                 double acc[8]) {
     const double c1 = __dmul_rn(__dsub_rn(q1[idx], start1), inv1);
     const double c2 = __dmul_rn(__dsub_rn(q2[idx], start2), inv2);
-    const double s1 = __dsub_rn(1.0, __dsub_rn(c1, (double)i1));
-    const double s2 = __dsub_rn(1.0, __dsub_rn(c2, (double)i2));
+    const double s1 = __dsub_rn(1.0, __dsub_rn(c1, fi1));
+    const double s2 = __dsub_rn(1.0, __dsub_rn(c2, fi2));
     const double t1 = __dsub_rn(1.0, s1), t2 = __dsub_rn(1.0, s2);
     const double wa = w0 ? w0[idx] : 1.0;
-    acc[0] = __dadd_rn(acc[0], __dmul_rn(__dmul_rn(wa, s1), s2));
-    acc[1] = __dadd_rn(acc[1], __dmul_rn(__dmul_rn(wa, s1), t2));
-    acc[2] = __dadd_rn(acc[2], __dmul_rn(__dmul_rn(wa, t1), s2));
-    acc[3] = __dadd_rn(acc[3], __dmul_rn(__dmul_rn(wa, t1), t2));
+    const double a1 = __dmul_rn(wa, s1), b1 = __dmul_rn(wa, t1);
+    acc[0] = __dadd_rn(acc[0], __dmul_rn(a1, s2));
+    acc[1] = __dadd_rn(acc[1], __dmul_rn(a1, t2));
+    acc[2] = __dadd_rn(acc[2], __dmul_rn(b1, s2));
+    acc[3] = __dadd_rn(acc[3], __dmul_rn(b1, t2));
     if (w1) {
         const double wb = w1[idx];
-        acc[4] = __dadd_rn(acc[4], __dmul_rn(__dmul_rn(wb, s1), s2));
-        acc[5] = __dadd_rn(acc[5], __dmul_rn(__dmul_rn(wb, s1), t2));
-        acc[6] = __dadd_rn(acc[6], __dmul_rn(__dmul_rn(wb, t1), s2));
-        acc[7] = __dadd_rn(acc[7], __dmul_rn(__dmul_rn(wb, t1), t2));
+        const double a2 = __dmul_rn(wb, s1), b2 = __dmul_rn(wb, t1);
+        acc[4] = __dadd_rn(acc[4], __dmul_rn(a2, s2));
+        acc[5] = __dadd_rn(acc[5], __dmul_rn(a2, t2));
+        acc[6] = __dadd_rn(acc[6], __dmul_rn(b2, s2));
+        acc[7] = __dadd_rn(acc[7], __dmul_rn(b2, t2));
     }
 }
 
-__global__ void __launch_bounds__(256)
-cell_sums(const uint32_t *__restrict__ vals, const uint32_t *__restrict__ cstart,
-          const uint32_t *__restrict__ cend, uint32_t nkeys, int nb2,
-          const double *__restrict__ q1, const double *__restrict__ q2,
-          const double *__restrict__ w0, const double *__restrict__ w1,
-          double start1, double inv1, double start2, double inv2,
-          double *__restrict__ partial) {
-    const uint32_t warp = (uint32_t)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    const uint32_t key0 = warp * 32u;
-    if (key0 >= nkeys) return;
-    const uint32_t key = key0 + (uint32_t)lane;
-    uint32_t b = 0, e = 0;
-    if (key < nkeys) { b = cstart[key]; e = cend[key]; }
-    const bool small = key < nkeys && e - b <= CELL_SMALL;
-    if (small) {
-        double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        const int i1 = (int)(key / (uint32_t)(nb2 + 1)) - 1;
-        const int i2 = (int)(key % (uint32_t)(nb2 + 1)) - 1;
-        for (uint32_t p = b; p < e; ++p)
-            cell_accumulate(vals[p], i1, i2, q1, q2, w0, w1, start1, inv1, start2, inv2, acc);
-        double2 *o = reinterpret_cast<double2 *>(partial + (size_t)key * 8);
-        o[0] = make_double2(acc[0], acc[1]);
-        o[1] = make_double2(acc[2], acc[3]);
-        o[2] = make_double2(acc[4], acc[5]);
-        o[3] = make_double2(acc[6], acc[7]);
+__device__ __forceinline__ void store8(double *dst, const double acc[8]) {
+    double2 *o = reinterpret_cast<double2 *>(dst);
+    o[0] = make_double2(acc[0], acc[1]);
+    o[1] = make_double2(acc[2], acc[3]);
+    o[2] = make_double2(acc[4], acc[5]);
+    o[3] = make_double2(acc[6], acc[7]);
+}
+
+// shared-memory slot of tile element i: one pad word per SEG_K so that the
+// threads of a warp, each reading its own SEG_K-run, hit distinct banks
+__device__ __forceinline__ int seg_slot(int i) { return i + i / SEG_K; }
+
+__global__ void __launch_bounds__(SEG_THREADS)
+seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, int64_t n,
+         uint32_t nkeys, int nb2, const uint32_t *__restrict__ cstart, const uint32_t *__restrict__ cend,
+         const double *__restrict__ q1, const double *__restrict__ q2,
+         const double *__restrict__ w0, const double *__restrict__ w1,
+         double start1, double inv1, double start2, double inv2,
+         double *__restrict__ partial, double *__restrict__ chunk_first, double *__restrict__ chunk_last) {
+    __shared__ uint32_t sk[SEG_TILE + SEG_TILE / SEG_K];
+    __shared__ uint32_t sv[SEG_TILE + SEG_TILE / SEG_K];
+    const int64_t base = (int64_t)blockIdx.x * SEG_TILE;
+    for (int i = threadIdx.x; i < SEG_TILE; i += SEG_THREADS) {
+        const int64_t g = base + i;
+        sk[seg_slot(i)] = g < n ? keys[g] : 0xffffffffu;
+        sv[seg_slot(i)] = g < n ? vals[g] : 0u;
     }
-    unsigned big = __ballot_sync(0xffffffffu, key < nkeys && !small);
-    while (big) {
-        const int l = __ffs(big) - 1;
-        big &= big - 1;
-        const uint32_t kk = key0 + (uint32_t)l;
-        const uint32_t bb = __shfl_sync(0xffffffffu, b, l), ee = __shfl_sync(0xffffffffu, e, l);
-        const int i1 = (int)(kk / (uint32_t)(nb2 + 1)) - 1;
-        const int i2 = (int)(kk % (uint32_t)(nb2 + 1)) - 1;
+    __syncthreads();
+    const int64_t t = (int64_t)blockIdx.x * SEG_THREADS + threadIdx.x;
+    const int64_t b = t * SEG_K;
+    const int64_t e = (b + SEG_K < n) ? b + SEG_K : n;
+    const int off = threadIdx.x * SEG_K;
+    int j = 0;
+    const int m = (int)(e > b ? e - b : 0);
+    while (j < m) {
+        const uint32_t k = sk[seg_slot(off + j)];
+        if (k >= nkeys) break;                     // outside-grid particles sort last
+        const double fi1 = (double)((int)(k / (uint32_t)(nb2 + 1)) - 1);
+        const double fi2 = (double)((int)(k % (uint32_t)(nb2 + 1)) - 1);
         double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (uint32_t p = bb + lane; p < ee; p += 32)
-            cell_accumulate(vals[p], i1, i2, q1, q2, w0, w1, start1, inv1, start2, inv2, acc);
+        const int j0 = j;
+        do {
+            cell_accumulate(sv[seg_slot(off + j)], fi1, fi2, q1, q2, w0, w1, start1, inv1, start2,
+                            inv2, acc);
+            ++j;
+        } while (j < m && sk[seg_slot(off + j)] == k);
+        const int64_t cs = cstart[k], ce = cend[k];
+        if (cs >= b && ce <= e) store8(partial + (size_t)k * 8, acc);
+        else if (j0 == 0) store8(chunk_first + (size_t)t * 8, acc);
+        else store8(chunk_last + (size_t)t * 8, acc);
+    }
+}
+
+__global__ void seg_combine(const uint32_t *__restrict__ cstart, const uint32_t *__restrict__ cend,
+                            uint32_t nkeys, const double *__restrict__ chunk_first,
+                            const double *__restrict__ chunk_last, double *__restrict__ partial) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nkeys) return;
+    const uint32_t cs = cstart[k], ce = cend[k];
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (ce == 0) {                                  // empty cell
+        store8(partial + (size_t)k * 8, acc);
+        return;
+    }
+    const uint32_t t0 = cs / SEG_K, t1 = (ce - 1) / SEG_K;
+    if (t0 == t1) return;                           // summed whole by seg_sums
+    const double *first = (cs == t0 * SEG_K) ? chunk_first : chunk_last;
 #pragma unroll
-        for (int c = 0; c < 8; ++c)
-            for (int o = 16; o > 0; o >>= 1) acc[c] = __dadd_rn(acc[c], __shfl_xor_sync(0xffffffffu, acc[c], o));
-        if (lane < 8) partial[(size_t)kk * 8 + lane] = acc[lane];
-    }
+    for (int c = 0; c < 8; ++c) acc[c] = first[(size_t)t0 * 8 + c];
+    for (uint32_t t = t0 + 1; t <= t1; ++t)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[c] = __dadd_rn(acc[c], chunk_first[(size_t)t * 8 + c]);
+    store8(partial + (size_t)k * 8, acc);
 }
 
 __global__ void cic_assemble(const double *__restrict__ partial, int nb1, int nb2,
@@ -372,10 +412,14 @@ static size_t deposit_carve(Carver &c, int64_t n, const DepositLayout &L, uint32
                             uint32_t **va, uint32_t **kb, uint32_t **vb, uint32_t **hist,
                             uint32_t **dtot, uint32_t **cs, uint32_t **ce, double **part) {
     const size_t nn = (size_t)(n > 0 ? n : 1);
-    *ka = c.take<uint32_t>(nn);
-    *va = c.take<uint32_t>(nn);
-    *kb = c.take<uint32_t>(nn);
-    *vb = c.take<uint32_t>(nn);
+    // the four sort buffers hold a multiple of SEG_K entries: after the sort
+    // the idle pair (4 B x that many each) is reused as the seg_sums chunk
+    // parts (8 doubles per SEG_K particles each)
+    const size_t nk = (nn + SEG_K - 1) / SEG_K * SEG_K;
+    *ka = c.take<uint32_t>(nk);
+    *va = c.take<uint32_t>(nk);
+    *kb = c.take<uint32_t>(nk);
+    *vb = c.take<uint32_t>(nk);
     *hist = c.take<uint32_t>((size_t)RS_BINS * L.ntiles);
     *dtot = c.take<uint32_t>(RS_BINS);
     *cs = c.take<uint32_t>((size_t)L.nkeys + 1);
@@ -473,9 +517,13 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
             t = vin; vin = vout; vout = t;
         }
         cell_ranges<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(kin, n, cs, ce);
-        const int64_t threads = (int64_t)L.nkeys * 32;
-        cell_sums<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
-            vin, cs, ce, L.nkeys, nb2, q1, q2, w0, w1, start1, inv1, start2, inv2, part);
+        double *cfirst = reinterpret_cast<double *>(kout);
+        double *clast = reinterpret_cast<double *>(vout);
+        seg_sums<<<(unsigned)((n + SEG_TILE - 1) / SEG_TILE), SEG_THREADS, 0, s>>>(
+            kin, vin, n, L.nkeys, nb2, cs, ce, q1, q2, w0, w1, start1, inv1, start2, inv2, part,
+            cfirst, clast);
+        seg_combine<<<(unsigned)((L.nkeys + 255) / 256), 256, 0, s>>>(cs, ce, L.nkeys, cfirst,
+                                                                       clast, part);
     } else {
         DFCSR_CUDA_TRY(cudaMemsetAsync(part, 0, sizeof(double) * (size_t)L.nkeys * 8, s));
     }
