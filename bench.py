@@ -232,6 +232,8 @@ def gpu_arm(a):
     # warm-up (builds the history; untimed)
     timed_steps(run, sets, 1, W, a.precision)
     barrier()
+    fma_peaks = measure_fma_peaks()
+    barrier()
     _lib.timing_reset()
     _lib.timing_enable(True)
     clocks = ClockSampler(local)
@@ -305,6 +307,7 @@ def gpu_arm(a):
                                           f"(5 fields x 8 corners), {per_launch_pts:.3g} points per "
                                           "launch; gathers are served mostly from L1/L2",
                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+    out["peaks_measured"] = fma_peaks
     out["gpu_launches"] = int(sum(launches.values()))
     out["kernel_launches_by_name"] = launches
     out["kernel_ms_per_step"] = kernel_ms
@@ -364,6 +367,33 @@ def gpu_arm(a):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(out))
+
+
+def measure_fma_peaks():
+    """FP32 and FP64 fused multiply-add throughput of this GPU (TFLOP/s),
+    measured with the library's probe kernel (best of 5, CUDA events)."""
+    import ctypes
+    import torch
+    from pydfcsr_gb300 import _lib
+    from pydfcsr_gb300.runtime import ptr, stream_handle
+    sink = torch.zeros(2, dtype=torch.float64, device="cuda")
+    out = {}
+    for name, fp64, iters in (("fp32_tflops", 0, 20000), ("fp64_tflops", 1, 600)):
+        flops = ctypes.c_double()
+        best = None
+        for rep in range(6):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.call("dfcsr_probe_fma", fp64, iters, ptr(sink), ctypes.byref(flops), stream_handle())
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            if rep > 0:
+                best = ms if best is None else min(best, ms)
+        out[name] = flops.value / (best * 1e-3) / 1e12
+    out["how"] = ("dfcsr_probe_fma: 8 independent FMA chains per thread, 4 x 256-thread blocks per "
+                  "SM, best of 5 launches timed with CUDA events")
+    return out
 
 
 def serving_leg(n_requests, rate_hz, fp64_sample, seed=4):

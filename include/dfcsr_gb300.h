@@ -271,6 +271,15 @@ int dfcsr_apply_wakes(double *coords, int64_t n, int64_t ld, const double *dE_dc
                       double init_energy, int transverse_on, void *workspace,
                       size_t workspace_bytes, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Arithmetic-rate probe (measurement only; no counterpart in the
+ * reference).  Launches a kernel of independent fused multiply-add chains in
+ * FP64 (fp64 != 0) or FP32 with `iters` iterations per thread and stores its
+ * floating-point operation count in *flops (host); time it with events on
+ * `stream` to get the FMA throughput.  `sink`: 8 bytes of device memory
+ * (never written in practice). */
+int dfcsr_probe_fma(int fp64, int64_t iters, void *sink, double *flops, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -126,6 +126,7 @@ _SIGS = [
     ("dfcsr_wake_mixed", _c_int, [_p, _p, _p, _p, _c_i64, _c_int, _c_int, _c_int, _p, _p, _p,
                                    _c_size, _p]),
     ("dfcsr_transport6", _c_int, [_p, _p, _c_i64, _c_i64, _p]),
+    ("dfcsr_probe_fma", _c_int, [_c_int, _c_i64, _p, ctypes.POINTER(_c_double), _p]),
     ("dfcsr_apply_wakes_workspace_bytes", _c_size, [_c_int, _c_int]),
     ("dfcsr_apply_wakes", _c_int, [_p, _c_i64, _c_i64, _p, _p, _p, _p, _c_int, _c_int, _c_double,
                                     _c_double, _c_double, _c_double, _c_int, _p, _c_size, _p]),

@@ -33,6 +33,7 @@ UNITS = {
     "dfstage.cu": [],
     "history.cu": [],
     "interp.cu": [],
+    "probe.cu": [],
     "wake_fp64.cu": ["-fmad=false"],
     "wake_mixed.cu": [],
 }

@@ -3,18 +3,30 @@
 // histogram_cic_2d (pyDFCSR_2D/deposit.py:43-87) scatters four corner weights
 // per particle serially.  Here particles are sorted by their lower cell with
 // a stable LSD radix sort (8-bit digits, per-warp match_any ranking, no
-// atomics), every lower cell is reduced by one warp in a fixed order into
-// eight partial sums (4 corners x 2 weight channels), and a gather pass adds
-// the four partials that land on each output cell.  Same result for the same
-// input on every run; no floating-point atomics anywhere.
+// atomics), fixed-size chunks of the sorted particles are reduced per lower
+// cell into four moments per weight channel (sum w, w f1, w f2, w f1 f2 of
+// the fractional offsets), and a gather pass forms the four corner sums that
+// land on each output cell.  Same result for the same input on every run; no
+// floating-point atomics anywhere.  GB300 runs FP64 at 1/64 of the FP32 rate,
+// so the per-particle FP64 work is kept to 6 (keys) + 13 (sums) operations.
 #include "dfcsr_common.cuh"
 
 namespace dfcsr {
 
 // ------------------------------------------------------------------ moments
+// Two passes over (x, z), each a grid-stride loop with per-block partial sums
+// and a one-block finish in a fixed order (deterministic).
+//   pass 1: sums of dx, dz, dx^2, dz^2, dx dz with d = value - first value
+//           (the shift keeps the variance free of cancellation for beams far
+//           from the origin) -> means, sigma_x, sigma_z, cov, least-squares
+//           slope and intercept of x on z (numpy.polyfit(z, x, 1));
+//   pass 2: the |z| < 0.1 sigma_z slice (count, sum and square sum of
+//           x - mean_x) and x_transform = x - (slope z + intercept) (sum and
+//           square sum) -> sigma_x of the slice, mean and sigma of x_transform.
+// FP64 operations per particle: 7 in pass 1, 8 in pass 2.
 constexpr int MOM_THREADS = 256;
 constexpr int MOM_MAX_BLOCKS = 1024;
-constexpr int MOM_K = 4;   // partial sums per pass
+constexpr int MOM_K = 5;   // partial sums per pass
 
 static int moment_blocks(int64_t n) {
     int64_t b = (n + MOM_THREADS * 8 - 1) / (MOM_THREADS * 8);
@@ -25,38 +37,47 @@ static int moment_blocks(int64_t n) {
 
 // stats layout (see header): 0 n, 1 mean_x, 2 mean_z, 3 sigma_x, 4 sigma_z,
 // 5 slope, 6 intercept, 7 n_slice, 8 sigma_x_slice, 9 mean_xt, 10 sigma_xt,
-// 11 cov_xz, 12 slice mean (internal), 13 sum_xx, 14 sum_zz, 15 sum_xz
+// 11 cov_xz, 12..15 reserved (zero)
 template <int PASS>
 __global__ void __launch_bounds__(MOM_THREADS)
 moments_pass(const double *__restrict__ x, const double *__restrict__ z, int64_t n,
              const double *__restrict__ stats, double *__restrict__ partial) {
     __shared__ double red[MOM_THREADS / 32];
-    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    double mx = 0, mz = 0, sz = 0, slope = 0, icpt = 0, ms = 0, mt = 0;
-    if (PASS >= 2) { mx = stats[1]; mz = stats[2]; }
-    if (PASS >= 3) { sz = stats[4]; slope = stats[5]; icpt = stats[6]; }
-    if (PASS >= 4) { ms = stats[12]; mt = stats[9]; }
+    double x0, z0, lim = 0, slope = 0, icpt = 0;
+    if (PASS == 1) {
+        x0 = x[0];
+        z0 = z[0];
+    } else {
+        x0 = stats[1];
+        z0 = 0.0;
+        lim = __dmul_rn(0.1, stats[4]);
+        slope = stats[5];
+        icpt = stats[6];
+    }
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const double xi = x[i], zi = z[i];
         if (PASS == 1) {
-            a0 += xi;
-            a1 += zi;
-        } else if (PASS == 2) {
-            const double dx = xi - mx, dz = zi - mz;
-            a0 += dx * dx;
-            a1 += dz * dz;
-            a2 += dx * dz;
-        } else if (PASS == 3) {
-            if (fabs(zi) < 0.1 * sz) { a0 += 1.0; a1 += xi; }
-            a2 += xi - (slope * zi + icpt);
+            const double dx = xi - x0, dz = zi - z0;
+            a0 += dx;
+            a1 += dz;
+            a2 = fma(dx, dx, a2);
+            a3 = fma(dz, dz, a3);
+            a4 = fma(dx, dz, a4);
         } else {
-            if (fabs(zi) < 0.1 * sz) { const double d = xi - ms; a0 += d * d; }
-            const double dt = (xi - (slope * zi + icpt)) - mt;
-            a1 += dt * dt;
+            if (fabs(zi) < lim) {
+                const double d = xi - x0;
+                a0 += 1.0;
+                a1 += d;
+                a2 = fma(d, d, a2);
+            }
+            const double xt = xi - fma(slope, zi, icpt);
+            a3 += xt;
+            a4 = fma(xt, xt, a4);
         }
     }
-    double v[MOM_K] = {a0, a1, a2, a3};
+    double v[MOM_K] = {a0, a1, a2, a3, a4};
     for (int k = 0; k < MOM_K; ++k) {
         const double s = block_sum(v[k], red);
         if (threadIdx.x == 0) partial[(size_t)blockIdx.x * MOM_K + k] = s;
@@ -65,7 +86,8 @@ moments_pass(const double *__restrict__ x, const double *__restrict__ z, int64_t
 
 template <int PASS>
 __global__ void __launch_bounds__(MOM_THREADS)
-moments_finish(const double *__restrict__ partial, int nblk, int64_t n, double *__restrict__ stats) {
+moments_finish(const double *__restrict__ x, const double *__restrict__ z,
+               const double *__restrict__ partial, int nblk, int64_t n, double *__restrict__ stats) {
     __shared__ double red[MOM_THREADS / 32];
     double tot[MOM_K];
     for (int k = 0; k < MOM_K; ++k) {
@@ -76,24 +98,26 @@ moments_finish(const double *__restrict__ partial, int nblk, int64_t n, double *
     if (threadIdx.x != 0) return;
     const double dn = (double)n;
     if (PASS == 1) {
+        const double mdx = tot[0] / dn, mdz = tot[1] / dn;
+        const double vx = fmax(tot[2] / dn - mdx * mdx, 0.0);
+        const double vz = fmax(tot[3] / dn - mdz * mdz, 0.0);
+        const double cov = tot[4] / dn - mdx * mdz;
         stats[0] = dn;
-        stats[1] = tot[0] / dn;
-        stats[2] = tot[1] / dn;
-    } else if (PASS == 2) {
-        stats[13] = tot[0]; stats[14] = tot[1]; stats[15] = tot[2];
-        stats[3] = sqrt(tot[0] / dn);
-        stats[4] = sqrt(tot[1] / dn);
-        stats[11] = tot[2] / dn;
-        const double slope = tot[2] / tot[1];
+        stats[1] = x[0] + mdx;
+        stats[2] = z[0] + mdz;
+        stats[3] = sqrt(vx);
+        stats[4] = sqrt(vz);
+        stats[11] = cov;
+        const double slope = cov / vz;
         stats[5] = slope;
         stats[6] = stats[1] - slope * stats[2];
-    } else if (PASS == 3) {
-        stats[7] = tot[0];
-        stats[12] = tot[1] / tot[0];          // NaN when the slice is empty
-        stats[9] = tot[2] / dn;
     } else {
-        stats[8] = sqrt(tot[0] / stats[7]);   // NaN when the slice is empty
-        stats[10] = sqrt(tot[1] / dn);
+        const double ms = tot[1] / tot[0];        // NaN when the slice is empty
+        stats[7] = tot[0];
+        stats[8] = sqrt(fmax(tot[2] / tot[0] - ms * ms, 0.0));
+        const double mt = tot[3] / dn;
+        stats[9] = mt;
+        stats[10] = sqrt(fmax(tot[4] / dn - mt * mt, 0.0));
     }
 }
 
@@ -101,19 +125,25 @@ moments_finish(const double *__restrict__ partial, int nblk, int64_t n, double *
 // Lower-cell key of a particle: (i1 + 1) * (nb2 + 1) + (i2 + 1) for
 // i1 in [-1, nb1 - 1], i2 in [-1, nb2 - 1]; particles with no corner inside
 // the grid get the sentinel nkeys and sort to the end.
+// The cell coordinate is the reference's (q - start) * inv_spacing; its
+// floor is taken by one round-toward-minus-infinity conversion (saturating
+// for huge or infinite values) and NaN coordinates are caught on the bit
+// pattern, so the FP64 pipe does six operations per particle.
+__device__ __forceinline__ bool is_nan_bits(double v) {
+    return (__double_as_longlong(v) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+
 __global__ void cic_keys(const double *__restrict__ q1, const double *__restrict__ q2, int64_t n,
                          int nb1, double start1, double inv1, int nb2, double start2, double inv2,
                          uint32_t nkeys, uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double c1 = __dmul_rn(__dsub_rn(q1[i], start1), inv1);
-    const double c2 = __dmul_rn(__dsub_rn(q2[i], start2), inv2);
-    const double f1 = floor(c1), f2 = floor(c2);
+    const double a = q1[i], b = q2[i];
+    const int i1 = __double2int_rd(__dmul_rn(__dsub_rn(a, start1), inv1));
+    const int i2 = __double2int_rd(__dmul_rn(__dsub_rn(b, start2), inv2));
     uint32_t key = nkeys;
-    if (f1 > -2.0 && f1 < (double)nb1 && f2 > -2.0 && f2 < (double)nb2) {
-        const int i1 = (int)f1, i2 = (int)f2;
+    if (i1 >= -1 && i1 < nb1 && i2 >= -1 && i2 < nb2 && !is_nan_bits(a) && !is_nan_bits(b))
         key = (uint32_t)(i1 + 1) * (uint32_t)(nb2 + 1) + (uint32_t)(i2 + 1);
-    }
     keys[i] = key;
     vals[i] = (uint32_t)i;
 }
@@ -272,29 +302,38 @@ constexpr int SEG_K = 16;
 constexpr int SEG_THREADS = 256;
 constexpr int SEG_TILE = SEG_K * SEG_THREADS;
 
+// Per-cell moments of the fractional offsets f = c - floor(c) for each
+// weight channel: [sum w, sum w f1, sum w f2, sum w f1 f2].  The CIC corner
+// weights (1 - f1)(1 - f2), (1 - f1) f2, f1 (1 - f2), f1 f2 are linear in
+// these, so cic_assemble forms the corner sums from the moments.  Per
+// particle: 6 FP64 operations for f1, f2 and 3 + 4 for the two channels
+// (channel 0 without weights counts particles as an integer).
+template <bool W0, bool W1>
 __device__ __forceinline__ void cell_accumulate(uint32_t idx, double fi1, double fi2,
                                                 const double *__restrict__ q1, const double *__restrict__ q2,
                                                 const double *__restrict__ w0, const double *__restrict__ w1,
                                                 double start1, double inv1, double start2, double inv2,
                                                 double acc[8]) {
-    const double c1 = __dmul_rn(__dsub_rn(q1[idx], start1), inv1);
-    const double c2 = __dmul_rn(__dsub_rn(q2[idx], start2), inv2);
-    const double s1 = __dsub_rn(1.0, __dsub_rn(c1, fi1));
-    const double s2 = __dsub_rn(1.0, __dsub_rn(c2, fi2));
-    const double t1 = __dsub_rn(1.0, s1), t2 = __dsub_rn(1.0, s2);
-    const double wa = w0 ? w0[idx] : 1.0;
-    const double a1 = __dmul_rn(wa, s1), b1 = __dmul_rn(wa, t1);
-    acc[0] = __dadd_rn(acc[0], __dmul_rn(a1, s2));
-    acc[1] = __dadd_rn(acc[1], __dmul_rn(a1, t2));
-    acc[2] = __dadd_rn(acc[2], __dmul_rn(b1, s2));
-    acc[3] = __dadd_rn(acc[3], __dmul_rn(b1, t2));
-    if (w1) {
-        const double wb = w1[idx];
-        const double a2 = __dmul_rn(wb, s1), b2 = __dmul_rn(wb, t1);
-        acc[4] = __dadd_rn(acc[4], __dmul_rn(a2, s2));
-        acc[5] = __dadd_rn(acc[5], __dmul_rn(a2, t2));
-        acc[6] = __dadd_rn(acc[6], __dmul_rn(b2, s2));
-        acc[7] = __dadd_rn(acc[7], __dmul_rn(b2, t2));
+    const double f1 = __dsub_rn(__dmul_rn(__dsub_rn(q1[idx], start1), inv1), fi1);
+    const double f2 = __dsub_rn(__dmul_rn(__dsub_rn(q2[idx], start2), inv2), fi2);
+    const double p = __dmul_rn(f1, f2);
+    if (W0) {
+        const double w = w0[idx];
+        acc[0] = __dadd_rn(acc[0], w);
+        acc[1] = __fma_rn(w, f1, acc[1]);
+        acc[2] = __fma_rn(w, f2, acc[2]);
+        acc[3] = __fma_rn(w, p, acc[3]);
+    } else {
+        acc[1] = __dadd_rn(acc[1], f1);
+        acc[2] = __dadd_rn(acc[2], f2);
+        acc[3] = __dadd_rn(acc[3], p);
+    }
+    if (W1) {
+        const double w = w1[idx];
+        acc[4] = __dadd_rn(acc[4], w);
+        acc[5] = __fma_rn(w, f1, acc[5]);
+        acc[6] = __fma_rn(w, f2, acc[6]);
+        acc[7] = __fma_rn(w, p, acc[7]);
     }
 }
 
@@ -310,6 +349,7 @@ __device__ __forceinline__ void store8(double *dst, const double acc[8]) {
 // threads of a warp, each reading its own SEG_K-run, hit distinct banks
 __device__ __forceinline__ int seg_slot(int i) { return i + i / SEG_K; }
 
+template <bool W0, bool W1>
 __global__ void __launch_bounds__(SEG_THREADS)
 seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, int64_t n,
          uint32_t nkeys, int nb2, const uint32_t *__restrict__ cstart, const uint32_t *__restrict__ cend,
@@ -340,10 +380,11 @@ seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, i
         double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         const int j0 = j;
         do {
-            cell_accumulate(sv[seg_slot(off + j)], fi1, fi2, q1, q2, w0, w1, start1, inv1, start2,
-                            inv2, acc);
+            cell_accumulate<W0, W1>(sv[seg_slot(off + j)], fi1, fi2, q1, q2, w0, w1, start1, inv1,
+                                    start2, inv2, acc);
             ++j;
         } while (j < m && sk[seg_slot(off + j)] == k);
+        if (!W0) acc[0] = (double)(j - j0);
         const int64_t cs = cstart[k], ce = cend[k];
         if (cs >= b && ce <= e) store8(partial + (size_t)k * 8, acc);
         else if (j0 == 0) store8(chunk_first + (size_t)t * 8, acc);
@@ -373,6 +414,14 @@ __global__ void seg_combine(const uint32_t *__restrict__ cstart, const uint32_t 
     store8(partial + (size_t)k * 8, acc);
 }
 
+// Corner sums of lower cell k from its moments m = [S, Sf1, Sf2, Sf1f2]:
+// 00 = S - Sf1 - Sf2 + Sf1f2, 01 = Sf2 - Sf1f2, 10 = Sf1 - Sf1f2, 11 = Sf1f2.
+__device__ __forceinline__ double corner00(const double *m) {
+    return __dadd_rn(__dsub_rn(__dsub_rn(m[0], m[1]), m[2]), m[3]);
+}
+__device__ __forceinline__ double corner01(const double *m) { return __dsub_rn(m[2], m[3]); }
+__device__ __forceinline__ double corner10(const double *m) { return __dsub_rn(m[1], m[3]); }
+
 __global__ void cic_assemble(const double *__restrict__ partial, int nb1, int nb2,
                              double *__restrict__ out0, double *__restrict__ out1) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -384,11 +433,14 @@ __global__ void cic_assemble(const double *__restrict__ partial, int nb1, int nb
     const size_t k01 = (size_t)(a + 1) * W + b;         // (a, b-1) -> its corner 01
     const size_t k10 = (size_t)a * W + (b + 1);         // (a-1, b) -> its corner 10
     const size_t k11 = (size_t)a * W + b;               // (a-1, b-1) -> its corner 11
-    out0[t] = __dadd_rn(__dadd_rn(__dadd_rn(partial[k00 * 8 + 0], partial[k01 * 8 + 1]),
-                                  partial[k10 * 8 + 2]), partial[k11 * 8 + 3]);
-    if (out1)
-        out1[t] = __dadd_rn(__dadd_rn(__dadd_rn(partial[k00 * 8 + 4], partial[k01 * 8 + 5]),
-                                      partial[k10 * 8 + 6]), partial[k11 * 8 + 7]);
+    for (int ch = 0; ch < (out1 ? 2 : 1); ++ch) {
+        const int o = 4 * ch;
+        const double v = __dadd_rn(__dadd_rn(__dadd_rn(corner00(partial + k00 * 8 + o),
+                                                        corner01(partial + k01 * 8 + o)),
+                                             corner10(partial + k10 * 8 + o)),
+                                   partial[k11 * 8 + o + 3]);
+        (ch ? out1 : out0)[t] = v;
+    }
 }
 
 struct DepositLayout {
@@ -452,13 +504,9 @@ extern "C" int dfcsr_beam_moments(const double *x, const double *z, int64_t n, d
     ScopedTiming tm("beam_moments", s);
     DFCSR_CUDA_TRY(cudaMemsetAsync(out, 0, 16 * sizeof(double), s));
     moments_pass<1><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
-    moments_finish<1><<<1, MOM_THREADS, 0, s>>>(part, nblk, n, out);
+    moments_finish<1><<<1, MOM_THREADS, 0, s>>>(x, z, part, nblk, n, out);
     moments_pass<2><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
-    moments_finish<2><<<1, MOM_THREADS, 0, s>>>(part, nblk, n, out);
-    moments_pass<3><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
-    moments_finish<3><<<1, MOM_THREADS, 0, s>>>(part, nblk, n, out);
-    moments_pass<4><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
-    moments_finish<4><<<1, MOM_THREADS, 0, s>>>(part, nblk, n, out);
+    moments_finish<2><<<1, MOM_THREADS, 0, s>>>(x, z, part, nblk, n, out);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }
@@ -519,9 +567,15 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
         cell_ranges<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(kin, n, cs, ce);
         double *cfirst = reinterpret_cast<double *>(kout);
         double *clast = reinterpret_cast<double *>(vout);
-        seg_sums<<<(unsigned)((n + SEG_TILE - 1) / SEG_TILE), SEG_THREADS, 0, s>>>(
-            kin, vin, n, L.nkeys, nb2, cs, ce, q1, q2, w0, w1, start1, inv1, start2, inv2, part,
-            cfirst, clast);
+        const unsigned sb = (unsigned)((n + SEG_TILE - 1) / SEG_TILE);
+#define DFCSR_SEG(A, B)                                                                       \
+    seg_sums<A, B><<<sb, SEG_THREADS, 0, s>>>(kin, vin, n, L.nkeys, nb2, cs, ce, q1, q2, w0, w1, \
+                                              start1, inv1, start2, inv2, part, cfirst, clast)
+        if (w0 && w1) DFCSR_SEG(true, true);
+        else if (w0) DFCSR_SEG(true, false);
+        else if (w1) DFCSR_SEG(false, true);
+        else DFCSR_SEG(false, false);
+#undef DFCSR_SEG
         seg_combine<<<(unsigned)((L.nkeys + 255) / 256), 256, 0, s>>>(cs, ce, L.nkeys, cfirst,
                                                                        clast, part);
     } else {
