@@ -370,25 +370,37 @@ seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, i
     const int64_t b = t * SEG_K;
     const int64_t e = (b + SEG_K < n) ? b + SEG_K : n;
     const int off = threadIdx.x * SEG_K;
-    int j = 0;
     const int m = (int)(e > b ? e - b : 0);
-    while (j < m) {
-        const uint32_t k = sk[seg_slot(off + j)];
-        if (k >= nkeys) break;                     // outside-grid particles sort last
-        const double fi1 = (double)((int)(k / (uint32_t)(nb2 + 1)) - 1);
-        const double fi2 = (double)((int)(k % (uint32_t)(nb2 + 1)) - 1);
-        double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        const int j0 = j;
-        do {
+    // Fixed trip count: every thread accumulates one particle per iteration,
+    // so the FP64 work runs on full warps; only the flush at the end of a
+    // run (integer work and stores) diverges.
+    uint32_t k = m > 0 ? sk[seg_slot(off)] : nkeys;
+    double fi1 = (double)((int)(k / (uint32_t)(nb2 + 1)) - 1);
+    double fi2 = (double)((int)(k % (uint32_t)(nb2 + 1)) - 1);
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int j0 = 0;
+#pragma unroll 1
+    for (int j = 0; j < SEG_K; ++j) {
+        const bool live = j < m && k < nkeys;      // outside-grid particles sort last
+        if (live)
             cell_accumulate<W0, W1>(sv[seg_slot(off + j)], fi1, fi2, q1, q2, w0, w1, start1, inv1,
                                     start2, inv2, acc);
-            ++j;
-        } while (j < m && sk[seg_slot(off + j)] == k);
-        if (!W0) acc[0] = (double)(j - j0);
-        const int64_t cs = cstart[k], ce = cend[k];
-        if (cs >= b && ce <= e) store8(partial + (size_t)k * 8, acc);
-        else if (j0 == 0) store8(chunk_first + (size_t)t * 8, acc);
-        else store8(chunk_last + (size_t)t * 8, acc);
+        const uint32_t kn = (j + 1 < m) ? sk[seg_slot(off + j + 1)] : 0xffffffffu;
+        if (live && kn != k) {                     // the run of key k ends at j
+            if (!W0) acc[0] = (double)(j + 1 - j0);
+            const int64_t cs = cstart[k], ce = cend[k];
+            if (cs >= b && ce <= e) store8(partial + (size_t)k * 8, acc);
+            else if (j0 == 0) store8(chunk_first + (size_t)t * 8, acc);
+            else store8(chunk_last + (size_t)t * 8, acc);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) acc[c] = 0.0;
+            j0 = j + 1;
+            k = kn;
+            if (k < nkeys) {
+                fi1 = (double)((int)(k / (uint32_t)(nb2 + 1)) - 1);
+                fi2 = (double)((int)(k % (uint32_t)(nb2 + 1)) - 1);
+            }
+        }
     }
 }
 

@@ -16,10 +16,12 @@
 //        |r - r'| = r0 + delta,  delta = D / (r0 + sqrt(r0^2 + D)),
 //        D = u (|n'|^2 u - 2 R0.n'),  u = x' - x'_ref   (no cancellation);
 //    history coordinates are an integer cell (from FP64) plus an FP32
-//    offset, so a grid index near 1000 keeps ~1e-7 cell resolution; gathers
-//    and the integrand are FP32 (density_x as a float-float pair in the far
-//    region, where its x' integral cancels), Kahan-compensated per-thread sums
-//    and a fixed-order FP64 block reduction.
+//    offset, so a grid index near 1000 keeps ~1e-7 cell resolution; the x'
+//    axis (index and weight) is resolved once per row in FP64; gathers and
+//    the integrand are FP32 (in the far region density_x, whose x' integral
+//    cancels, is read as a stored hi + lo pair and interpolated in offset
+//    form so that it is rounded once), Kahan-compensated per-thread sums and
+//    a fixed-order FP64 block reduction.
 //  * band kernel (FP64, optional): s' columns with |s' - s| < near_band are
 //    skipped by the integral kernel and evaluated with the FP64 integrand.
 //  * finalize kernel: adds the regions in the reference's order and scales.
@@ -44,7 +46,7 @@ constexpr int RW = 8;
 //  3: |tau'|^2 (h), K0x = b - a e, K1x - 1 = a g - 1 + b e, K2x = b g
 //  4: K0z = a (1 - h), K1z = a e + b h, K2z = b e, Q0 = R0.(n - n')
 //  5: Q1 = n'.(n - n'), q2 = n.tau', M0 = Q0 - q2 |R0|, trapz weight in s'
-// row record words: x cell (int), x offset, u = x' - x'_ref, x' | trapz weight in x'
+// row record words: x0 (int), x weight, u = x' - x'_ref, x' | trapz weight in x', x1 - x0 (int)
 
 struct RegionMeta {
     int nxp, nsp, col_off, row_off;   // offsets in words within the point record
@@ -103,15 +105,19 @@ __device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *
 struct GeoShared {
     Region reg[WAKE_MAX_REGIONS];
     RegionMeta rm[WAKE_MAX_REGIONS];
+    Axis ax_s[WAKE_MAX_REGIONS], ax_x[WAKE_MAX_REGIONS];
+    double xref[WAKE_MAX_REGIONS];
+    int col_begin[WAKE_MAX_REGIONS + 1], row_begin[WAKE_MAX_REGIONS + 1];
+    int lo[WAKE_MAX_REGIONS], hi[WAKE_MAX_REGIONS];
     double lat_s[6];
     double vx_obs;
     int nreg, ok;
-    int lo, hi;
 };
 
 // One CTA per observation point: the per-point constants (regions, orbit at
-// s, vx at the observer) once in thread 0, then every region's s' columns and
-// x' rows across the block.
+// s, vx at the observer) once in thread 0, then the s' columns of all regions
+// as one flat range across the block (full warps for the FP64 work), then
+// the x' rows likewise.
 __global__ void __launch_bounds__(GEO_THREADS)
 mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
                const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
@@ -137,6 +143,21 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         gs.vx_obs = hist_field_fp64(J, 3, t, x, s - t);
         obs_vx[b] = gs.vx_obs;
         lattice_lerp(J, s, gs.lat_s);
+        int cb = 0, rb = 0;
+        for (int r = 0; r < gs.nreg; ++r) {
+            const Region &R = gs.reg[r];
+            gs.ax_s[r] = make_axis(R.sl, R.sr, R.nsp);
+            gs.ax_x[r] = make_axis(R.xl, R.xr, R.nxp);
+            gs.xref[r] = gs.ax_x[r].at(R.nxp / 2);
+            gs.col_begin[r] = cb;
+            gs.row_begin[r] = rb;
+            gs.lo[r] = R.nxp;
+            gs.hi[r] = -1;
+            cb += R.nsp;
+            rb += R.nxp;
+        }
+        gs.col_begin[gs.nreg] = cb;
+        gs.row_begin[gs.nreg] = rb;
     }
     __syncthreads();
     if (!gs.ok) return;
@@ -145,79 +166,82 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
     const double inv_s = 1.0 / J.s_delta, inv_t = 1.0 / J.t_delta, inv_z = 1.0 / J.z_delta;
     const double inv_x = 1.0 / J.x_delta;
     const int nreg = gs.nreg;
-    for (int r = 0; r < nreg; ++r) {
-        const Region R = gs.reg[r];
-        const Axis ax_s = make_axis(R.sl, R.sr, R.nsp);
-        const Axis ax_x = make_axis(R.xl, R.xr, R.nxp);
-        const double xref = ax_x.at(R.nxp / 2);
-        float4 *cb = reinterpret_cast<float4 *>(rec + (size_t)b * rec_words + gs.rm[r].col_off);
-        for (int j = threadIdx.x; j < R.nsp; j += blockDim.x) {
-            const double spj = ax_s.at(j);
-            // orbit tables at s' (interpolate1D rule, index by multiplication)
-            double L[6];
-            {
-                int a0, a1;
-                double f;
-                if (axis_index((spj - J.s_min) * inv_s, J.nsample, a0, a1, f)) {
-                    const double *pa = J.lattice + (size_t)a0 * 6, *pb = J.lattice + (size_t)a1 * 6;
+    float *prec = rec + (size_t)b * rec_words;
+    const int ncols = gs.col_begin[nreg];
+    for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+        int r = 0;
+        while (r + 1 < nreg && c >= gs.col_begin[r + 1]) ++r;
+        const int j = c - gs.col_begin[r];
+        const Axis ax_s = gs.ax_s[r];
+        const double xref = gs.xref[r];
+        const double spj = ax_s.at(j);
+        // orbit tables at s' (interpolate1D rule, index by multiplication)
+        double L[6];
+        {
+            int a0, a1;
+            double f;
+            if (axis_index((spj - J.s_min) * inv_s, J.nsample, a0, a1, f)) {
+                const double *pa = J.lattice + (size_t)a0 * 6, *pb = J.lattice + (size_t)a1 * 6;
 #pragma unroll
-                    for (int k = 0; k < 6; ++k) L[k] = fma(f, pb[k] - pa[k], pa[k]);
-                } else {
+                for (int k = 0; k < 6; ++k) L[k] = fma(f, pb[k] - pa[k], pa[k]);
+            } else {
 #pragma unroll
-                    for (int k = 0; k < 6; ++k) L[k] = 0.0;
-                }
-            }
-            const double npx = L[2], npy = L[3], tpx = L[4], tpy = L[5];
-            const double Ax = X0s - L[0] + x * nsx, Ay = Y0s - L[1] + x * nsy;
-            const double rx0 = Ax - xref * npx, ry0 = Ay - xref * npy;
-            const double r0 = sqrt(rx0 * rx0 + ry0 * ry0);
-            const double ut0 = (t - r0 - J.t_min) * inv_t;
-            const double uz0 = (spj - (t - r0) - J.z_min) * inv_z;
-            const double tfl = floor(ut0), zfl = floor(uz0);
-            const double a = vxo * tpx + vyo * tpy, bb = vxo * npx + vyo * npy;
-            const double e = tpx * npx + tpy * npy, g = npx * npx + npy * npy;
-            const double h = tpx * tpx + tpy * tpy;
-            const double nmx = nsx - npx, nmy = nsy - npy;
-            const double Q0 = rx0 * nmx + ry0 * nmy;
-            const double q2 = nsx * tpx + nsy * tpy;
-            const bool near = J.near_band > 0.0 && fabs(spj - s) < J.near_band;
-            float4 *o = cb + (size_t)j * (CW / 4);
-            o[0] = make_float4(__int_as_float(clamp_int(tfl)), __int_as_float(clamp_int(zfl)),
-                               (float)(ut0 - tfl), (float)(uz0 - zfl));
-            o[1] = make_float4((float)r0, (float)(rx0 * npx + ry0 * npy), (float)(g - 1.0),
-                               (float)rho_at(J, spj));
-            o[2] = make_float4((float)a, (float)bb, (float)e, (float)g);
-            o[3] = make_float4((float)h, (float)(bb - a * e), (float)((a * g - 1.0) + bb * e),
-                               (float)(bb * g));
-            o[4] = make_float4((float)(a * (1.0 - h)), (float)(a * e + bb * h), (float)(bb * e),
-                               (float)Q0);
-            o[5] = make_float4((float)(npx * nmx + npy * nmy), (float)q2, (float)(Q0 - q2 * r0),
-                               near ? 0.f : (float)ax_s.weight(j));   // band columns: FP64 kernel
-        }
-        // rows: x cell, offset, u = x' - x'_ref, x', trapz weight; valid row range
-        if (threadIdx.x == 0) { gs.lo = R.nxp; gs.hi = -1; }
-        __syncthreads();
-        float4 *rb = reinterpret_cast<float4 *>(rec + (size_t)b * rec_words + gs.rm[r].row_off);
-        const double ux_first = (R.xl - J.x_min) * inv_x, dux = ax_x.step * inv_x;
-        int lo = R.nxp, hi = -1;
-        for (int i = threadIdx.x; i < R.nxp; i += blockDim.x) {
-            const double xpi = ax_x.at(i);
-            const double ux = fma((double)i, dux, ux_first);
-            const double fb = floor(ux);
-            rb[2 * i] = make_float4(__int_as_float(clamp_int(fb)), (float)(ux - fb), (float)(xpi - xref),
-                                    (float)xpi);
-            rb[2 * i + 1] = make_float4((float)ax_x.weight(i), 0.f, 0.f, 0.f);
-            if (ux > -1.0 && ux < (double)J.nx) {
-                lo = min(lo, i);
-                hi = max(hi, i);
+                for (int k = 0; k < 6; ++k) L[k] = 0.0;
             }
         }
-        atomicMin(&gs.lo, lo);   // integer min / max: order independent
-        atomicMax(&gs.hi, hi);
-        __syncthreads();
-        if (threadIdx.x == 0) rows_valid[b * WAKE_MAX_REGIONS + r] = make_int2(gs.lo, gs.hi + 1);
-        __syncthreads();
+        const double npx = L[2], npy = L[3], tpx = L[4], tpy = L[5];
+        const double Ax = X0s - L[0] + x * nsx, Ay = Y0s - L[1] + x * nsy;
+        const double rx0 = Ax - xref * npx, ry0 = Ay - xref * npy;
+        const double r0 = sqrt(rx0 * rx0 + ry0 * ry0);
+        const double ut0 = (t - r0 - J.t_min) * inv_t;
+        const double uz0 = (spj - (t - r0) - J.z_min) * inv_z;
+        const double tfl = floor(ut0), zfl = floor(uz0);
+        const double a = vxo * tpx + vyo * tpy, bb = vxo * npx + vyo * npy;
+        const double e = tpx * npx + tpy * npy, g = npx * npx + npy * npy;
+        const double h = tpx * tpx + tpy * tpy;
+        const double nmx = nsx - npx, nmy = nsy - npy;
+        const double Q0 = rx0 * nmx + ry0 * nmy;
+        const double q2 = nsx * tpx + nsy * tpy;
+        const bool near = J.near_band > 0.0 && fabs(spj - s) < J.near_band;
+        float4 *o = reinterpret_cast<float4 *>(prec + gs.rm[r].col_off) + (size_t)j * (CW / 4);
+        o[0] = make_float4(__int_as_float(clamp_int(tfl)), __int_as_float(clamp_int(zfl)),
+                           (float)(ut0 - tfl), (float)(uz0 - zfl));
+        o[1] = make_float4((float)r0, (float)(rx0 * npx + ry0 * npy), (float)(g - 1.0),
+                           (float)rho_at(J, spj));
+        o[2] = make_float4((float)a, (float)bb, (float)e, (float)g);
+        o[3] = make_float4((float)h, (float)(bb - a * e), (float)((a * g - 1.0) + bb * e),
+                           (float)(bb * g));
+        o[4] = make_float4((float)(a * (1.0 - h)), (float)(a * e + bb * h), (float)(bb * e),
+                           (float)Q0);
+        o[5] = make_float4((float)(npx * nmx + npy * nmy), (float)q2, (float)(Q0 - q2 * r0),
+                           near ? 0.f : (float)ax_s.weight(j));   // band columns: FP64 kernel
     }
+    // rows: x cell, offset, u = x' - x'_ref, x', trapz weight; valid row range
+    const int nrows = gs.row_begin[nreg];
+    for (int c = threadIdx.x; c < nrows; c += blockDim.x) {
+        int r = 0;
+        while (r + 1 < nreg && c >= gs.row_begin[r + 1]) ++r;
+        const int i = c - gs.row_begin[r];
+        const Axis ax_x = gs.ax_x[r];
+        const double xpi = ax_x.at(i);
+        const double ux = fma((double)i, ax_x.step * inv_x, (gs.reg[r].xl - J.x_min) * inv_x);
+        // x axis of the history with the reference's rule (interpolate3D:
+        // in range iff -1 < u < nx, lower index int(u), weight u - int(u));
+        // rows in range form one contiguous run because u grows with i
+        int x0 = 0, x1 = 0;
+        double xw = 0.0;
+        const bool in = axis_index(ux, J.nx, x0, x1, xw);
+        float4 *rb = reinterpret_cast<float4 *>(prec + gs.rm[r].row_off);
+        rb[2 * i] = make_float4(__int_as_float(x0), (float)xw, (float)(xpi - gs.xref[r]), (float)xpi);
+        rb[2 * i + 1] = make_float4((float)ax_x.weight(i), __int_as_float(x1 - x0), 0.f, 0.f);
+        if (in) {
+            atomicMin(&gs.lo[r], i);   // integer min / max: order independent
+            atomicMax(&gs.hi[r], i);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < nreg)
+        rows_valid[b * WAKE_MAX_REGIONS + threadIdx.x] = make_int2(gs.lo[threadIdx.x], gs.hi[threadIdx.x] + 1);
 }
 
 // Resolve one axis from an integer base and an FP32 offset with the
@@ -236,28 +260,6 @@ __device__ __forceinline__ bool axis_split(int base, float off, int n, int &i0, 
 struct Fields5 {
     float den, dx, dz, vx, vxx;
 };
-
-// Error-free transformations (round-to-nearest intrinsics: never contracted).
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// Linear interpolation a + w (b - a) of float-float values (hi, lo).
-__device__ __forceinline__ float2 lerp_ff(float2 A, float2 B, float w) {
-    float dh, de;
-    two_sum(B.x, -A.x, dh, de);
-    const float dl = __fadd_rn(de, __fsub_rn(B.y, A.y));
-    const float ph = __fmul_rn(w, dh);
-    const float pe = __fmaf_rn(w, dh, -ph);
-    const float pl = __fmaf_rn(w, dl, pe);
-    float rh, re;
-    two_sum(A.x, ph, rh, re);
-    const float rl = __fadd_rn(re, __fadd_rn(A.y, pl));
-    const float s = __fadd_rn(rh, rl);
-    return make_float2(s, __fsub_rn(rl, __fsub_rn(s, rh)));
-}
 
 // a + w (b - a) with one rounding for the product-add.
 __device__ __forceinline__ float lerp1(float a, float b, float w) { return fmaf(w, b - a, a); }
@@ -294,14 +296,16 @@ __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint
     r.vx = tri(A0.w, B0.w, A1.w, B1.w, C0.w, D0.w, C1.w, D1.w);
     r.vxx = tri(a0.x, b0.x, a1.x, b1.x, c0.x, d0.x, c1.x, d1.x);
     if (FF) {
-        const float2 c00_ = lerp_ff(make_float2(A0.y, a0.y), make_float2(B0.y, b0.y), td);
-        const float2 c01_ = lerp_ff(make_float2(A1.y, a1.y), make_float2(B1.y, b1.y), td);
-        const float2 c10_ = lerp_ff(make_float2(C0.y, c0.y), make_float2(D0.y, d0.y), td);
-        const float2 c11_ = lerp_ff(make_float2(C1.y, c1.y), make_float2(D1.y, d1.y), td);
-        const float2 e0 = lerp_ff(c00_, c10_, xd);
-        const float2 e1 = lerp_ff(c01_, c11_, xd);
-        const float2 f = lerp_ff(e0, e1, zd);
-        r.dx = __fadd_rn(f.x, f.y);
+        // density_x stored as hi + lo: interpolate the offsets from the high
+        // part of the first corner, (hi_c - h) + lo_c (the subtraction is
+        // exact for neighbouring values within a factor 2), so the lerp
+        // chain rounds only small numbers and the result h + D is rounded
+        // once - a correctly rounded FP32 value of the FP64 interpolant
+        const float h = A0.y;
+        r.dx = __fadd_rn(h, tri(a0.y, __fadd_rn(__fsub_rn(B0.y, h), b0.y),
+                                __fadd_rn(__fsub_rn(A1.y, h), a1.y), __fadd_rn(__fsub_rn(B1.y, h), b1.y),
+                                __fadd_rn(__fsub_rn(C0.y, h), c0.y), __fadd_rn(__fsub_rn(D0.y, h), d0.y),
+                                __fadd_rn(__fsub_rn(C1.y, h), c1.y), __fadd_rn(__fsub_rn(D1.y, h), d1.y)));
     } else {
         r.dx = tri(A0.y + a0.y, B0.y + b0.y, A1.y + a1.y, B1.y + b1.y, C0.y + c0.y, D0.y + d0.y,
                    C1.y + c1.y, D1.y + d1.y);
@@ -345,7 +349,8 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const RingV
         const float4 *rr = sm.row + (i_lo + i) * (RW / 4);
         const float4 q0 = cr[0], q5 = cr[5];
         const float4 ra = rr[0];
-        const float wx = rr[1].x;
+        const float4 rw = rr[1];
+        const float wx = rw.x;
         const float ws = q5.w;
         i += di;
         jl += dj;
@@ -357,18 +362,20 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const RingV
         const float Dd = u * ((g1.z + 1.f) * u - 2.f * g1.y);
         const float rad = fmaf(r0, r0, Dd);
         const float delta = __fdividef(Dd, r0 + rad * rsqrtf(rad));
-        int t0, t1, x0, x1, z0, z1;
-        float td, xd, zd;
+        int t0, t1, z0, z1;
+        float td, zd;
         if (!axis_split(__float_as_int(q0.x), q0.z - delta * V.inv_dt, V.nt, t0, t1, td) ||
-            !axis_split(__float_as_int(ra.x), ra.y, V.nx, x0, x1, xd) ||
             !axis_split(__float_as_int(q0.y), q0.w + delta * V.inv_dz, V.nz, z0, z1, zd))
             continue;   // every field is zero outside the history grid
+        // x: rows outside the history grid are not in [i_lo, i_hi)
+        const int x0 = __float_as_int(ra.x);
+        const float xd = ra.y;
         int s0 = V.head + t0, s1 = V.head + t1;
         if (s0 >= V.cap) s0 -= V.cap;
         if (s1 >= V.cap) s1 -= V.cap;
         const uint32_t c0x0 = ((uint32_t)s0 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
         const uint32_t c1x0 = ((uint32_t)s1 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
-        const uint32_t dxc = (uint32_t)(x1 - x0) * nzc;
+        const uint32_t dxc = (uint32_t)__float_as_int(rw.y) * nzc;
         const Fields5 F = gather5<FF>(V.ring, c0x0, c1x0, c0x0 + dxc, c1x0 + dxc,
                                       2u * (uint32_t)(z1 - z0), td, xd, zd);
         const float4 q2 = cr[2], q3 = cr[3], q4 = cr[4];
