@@ -162,7 +162,6 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True):
     """Run steps first..first+count-1 from device-resident particle sets;
     ``events`` (list) receives one (start, end) CUDA event pair per step."""
     import torch
-    from pydfcsr_gb300.runtime import as_device_f64
     csr = run.csr
     stream = torch.cuda.current_stream()
     for k in range(first, first + count):
@@ -177,8 +176,7 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True):
         csr.update_history(lf)
         if wake:
             csr.get_CSR_mesh()
-            s = as_device_f64(run.beam.position + csr.CSR_zmesh)
-            x = as_device_f64(csr.CSR_xmesh)
+            s, x = csr.mesh_device()
             run.last = csr.wake_device(s, x, precision)
         if events is not None:
             ev[1].record(stream)

@@ -163,6 +163,16 @@ int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, double *vx,
  * (density_x - (double)(float)density_x), slots 6..7 zero.  Field order:
  * density, density_x, density_z, vx, vx_x.
  */
+/* The axis tables of dfcsr_history_regrid when the source grid and the
+ * target grid are numpy linspaces (get_DF's x_grids / z_grids and
+ * append_interpolant's x_grid_interp / z_grid_interp, deposit.py:170-171,
+ * 347-350): idx[ntgt], w[ntgt], oob[ntgt] computed on the device with the
+ * RegularGridInterpolator rule above, equal to the host computation from the
+ * numpy arrays. */
+int dfcsr_rgi_axis_linspace(double src_start, double src_stop, int nsrc,
+                            double tgt_start, double tgt_stop, int ntgt, int32_t *idx,
+                            double *w, uint8_t *oob, void *stream);
+
 int dfcsr_history_regrid(const double *density, const double *density_x,
                          const double *density_z, const double *vx,
                          const double *vx_x, int snx, int snz,
@@ -221,6 +231,14 @@ typedef struct {
 int dfcsr_wake_fp64(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
                     const double *s, const double *x, int64_t n,
                     double *dE, double *xkick, void *stream);
+
+/* Observation points of get_CSR_mesh + calculate_2D_CSR (CSR.py:361-418):
+ * zrange = linspace(z0, z1, zbins), xrange = linspace(x0, x1, xbins) (numpy's
+ * formula), point k = i * zbins + j: s[k] = position + zrange[j],
+ * x[k] = xrange[i] + (slope0 * zrange[j] + slope1).  s, x: [xbins * zbins]. */
+int dfcsr_csr_mesh(double x0, double x1, int xbins, double z0, double z1, int zbins,
+                   double slope0, double slope1, double position, double *s, double *x,
+                   void *stream);
 
 /* get_CSR_integrand (CSR.py:605-782) at m arbitrary points (sp[k], xp[k])
  * for one observation point (s, x) of *job (device pointer), plain FP64.

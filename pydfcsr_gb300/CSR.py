@@ -124,6 +124,8 @@ class CSR2D:
         self.parallel = False
         self.evaluator = WakeEvaluator(workspace)
         self._jobs_dev = None
+        self._mesh = None
+        self._mesh_host = None
         if beam is not None:
             self.initialization()
 
@@ -159,22 +161,51 @@ class CSR2D:
 
     # --------------------------------------------------------------- mesh
     def get_CSR_mesh(self):
-        """Observation mesh in chirp-removed coordinates (CSR.py:361-394)."""
+        """Observation mesh in chirp-removed coordinates (CSR.py:361-394).
+
+        Stores the mesh parameters; the host arrays (``CSR_xmesh``,
+        ``CSR_zmesh``, ``CSR_zrange``, ``CSR_xrange_transformed``) are built
+        with numpy on first access, and :meth:`mesh_device` builds the same
+        points on the GPU (bit for bit: numpy's linspace and polyval
+        arithmetic)."""
         b = self.beam
         p = b.slope
         sig_x, mean_x = b.sigma_x_transform, b.mean_x_transform
         sig_z, mean_z = b.sigma_z, b.mean_z
         xlim, zlim = self.CSR_params.xlim, self.CSR_params.zlim
-        xbins, zbins = self.CSR_params.xbins, self.CSR_params.zbins
-        zrange = np.linspace(mean_z - zlim * sig_z, mean_z + zlim * sig_z, zbins)
-        xrange = np.linspace(mean_x - xlim * sig_x, mean_x + xlim * sig_x, xbins)
-        xmesh_t, zmesh = np.meshgrid(xrange, zrange, indexing="ij")
-        xmesh_t = xmesh_t.flatten()
-        zmesh = zmesh.flatten()
-        self.CSR_xmesh = xmesh_t + np.polyval(p, zmesh)
-        self.CSR_zmesh = zmesh
-        self.CSR_zrange = zrange
-        self.CSR_xrange_transformed = xrange
+        xbins, zbins = int(self.CSR_params.xbins), int(self.CSR_params.zbins)
+        self._mesh = (mean_x - xlim * sig_x, mean_x + xlim * sig_x, xbins,
+                      mean_z - zlim * sig_z, mean_z + zlim * sig_z, zbins,
+                      float(p[0]), float(p[1]), float(b.position))
+        self._mesh_host = None
+
+    def _host_mesh(self):
+        if self._mesh_host is None:
+            x0, x1, xbins, z0, z1, zbins, p0, p1, _ = self._mesh
+            zrange = np.linspace(z0, z1, zbins)
+            xrange = np.linspace(x0, x1, xbins)
+            xmesh_t, zmesh = np.meshgrid(xrange, zrange, indexing="ij")
+            xmesh_t = xmesh_t.flatten()
+            zmesh = zmesh.flatten()
+            self._mesh_host = (xmesh_t + np.polyval(np.array([p0, p1]), zmesh), zmesh, zrange,
+                               xrange)
+        return self._mesh_host
+
+    CSR_xmesh = property(lambda self: self._host_mesh()[0])
+    CSR_zmesh = property(lambda self: self._host_mesh()[1])
+    CSR_zrange = property(lambda self: self._host_mesh()[2])
+    CSR_xrange_transformed = property(lambda self: self._host_mesh()[3])
+
+    def mesh_device(self, stream=None):
+        """(s, x) of every mesh point as float64 CUDA tensors, point k =
+        i * zbins + j like ``position + CSR_zmesh`` and ``CSR_xmesh``."""
+        x0, x1, xbins, z0, z1, zbins, p0, p1, _ = self._mesh
+        dev = torch.device("cuda", torch.cuda.current_device())
+        s = torch.empty(xbins * zbins, dtype=torch.float64, device=dev)
+        x = torch.empty(xbins * zbins, dtype=torch.float64, device=dev)
+        _lib.call("dfcsr_csr_mesh", x0, x1, xbins, z0, z1, zbins, p0, p1,
+                  float(self.beam.position), ptr(s), ptr(x), stream_handle(stream))
+        return s, x
 
     # --------------------------------------------------------------- wake
     def _job(self, position=None):
@@ -207,8 +238,7 @@ class CSR2D:
 
     def calculate_2D_CSR(self, precision=None):
         """Wake on the whole observation mesh (CSR.py:397-418)."""
-        s = as_device_f64(self.beam.position + self.CSR_zmesh)
-        x = as_device_f64(self.CSR_xmesh)
+        s, x = self.mesh_device()
         dE, xk = self.wake_device(s, x, precision)
         shape = (self.CSR_params.xbins, self.CSR_params.zbins)
         self.dE_dct = dE.cpu().numpy().reshape(shape)

@@ -116,6 +116,8 @@ _SIGS = [
                                     _c_size, _p]),
     ("dfcsr_history_regrid", _c_int, [_p, _p, _p, _p, _p, _c_int, _c_int, _p, _p, _p, _c_int,
                                        _p, _p, _p, _c_int, _p, _p, _p, _p]),
+    ("dfcsr_rgi_axis_linspace", _c_int, [_c_double, _c_double, _c_int, _c_double, _c_double,
+                                          _c_int, _p, _p, _p, _p]),
     ("dfcsr_interp3d", _c_int, [_p, _p, _p, _c_i64, _p, _c_int, _c_int, _c_int, _c_double,
                                  _c_double, _c_double, _c_double, _c_double, _c_double, _p, _p]),
     ("dfcsr_interp1d", _c_int, [_p, _c_i64, _p, _c_int, _c_double, _c_double, _p, _p]),
@@ -125,6 +127,8 @@ _SIGS = [
     ("dfcsr_wake_workspace_bytes", _c_size, [_c_int, _c_int, _c_i64]),
     ("dfcsr_wake_mixed", _c_int, [_p, _p, _p, _p, _c_i64, _c_int, _c_int, _c_int, _p, _p, _p,
                                    _c_size, _p]),
+    ("dfcsr_csr_mesh", _c_int, [_c_double, _c_double, _c_int, _c_double, _c_double, _c_int,
+                                 _c_double, _c_double, _c_double, _p, _p, _p]),
     ("dfcsr_transport6", _c_int, [_p, _p, _c_i64, _c_i64, _p]),
     ("dfcsr_probe_fma", _c_int, [_c_int, _c_i64, _p, ctypes.POINTER(_c_double), _p]),
     ("dfcsr_apply_wakes_workspace_bytes", _c_size, [_c_int, _c_int]),

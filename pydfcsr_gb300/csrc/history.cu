@@ -65,9 +65,48 @@ __global__ void regrid5(const double *__restrict__ f0, const double *__restrict_
     }
 }
 
+// RegularGridInterpolator axis tables for a source grid and a target grid
+// that are both numpy linspaces: i = clip(searchsorted(src, t, 'right') - 1,
+// 0, ns - 2), w = (t - src[i]) / (src[i+1] - src[i]), oob = t < src[0] or
+// t > src[ns-1].  Grid values are regenerated with numpy's linspace formula,
+// so the tables equal the ones computed from the host arrays.
+__global__ void rgi_axis_linspace(double s0, double s1, int ns, double t0, double t1, int nt,
+                                  int32_t *__restrict__ idx, double *__restrict__ w,
+                                  uint8_t *__restrict__ oob) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nt) return;
+    const double t = np_linspace_at(t0, t1, nt, m);
+    int lo = 0, hi = ns;                      // count of src values <= t
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (np_linspace_at(s0, s1, ns, mid) <= t) lo = mid + 1;
+        else hi = mid;
+    }
+    int i = lo - 1;
+    if (i < 0) i = 0;
+    if (i > ns - 2) i = ns - 2;
+    const double a = np_linspace_at(s0, s1, ns, i), b = np_linspace_at(s0, s1, ns, i + 1);
+    idx[m] = i;
+    w[m] = __ddiv_rn(__dsub_rn(t, a), __dsub_rn(b, a));
+    oob[m] = (t < np_linspace_at(s0, s1, ns, 0) || t > np_linspace_at(s0, s1, ns, ns - 1)) ? 1 : 0;
+}
+
 }  // namespace dfcsr
 
 using namespace dfcsr;
+
+extern "C" int dfcsr_rgi_axis_linspace(double src_start, double src_stop, int nsrc,
+                                       double tgt_start, double tgt_stop, int ntgt, int32_t *idx,
+                                       double *w, uint8_t *oob, void *stream) {
+    clear_error();
+    DFCSR_CHECK_ARG(nsrc >= 2 && ntgt >= 1, "dfcsr_rgi_axis_linspace: need nsrc >= 2, ntgt >= 1");
+    DFCSR_CHECK_ARG(idx && w && oob, "dfcsr_rgi_axis_linspace: null pointer");
+    DFCSR_CHECK_ARG(src_stop > src_start, "dfcsr_rgi_axis_linspace: source grid must ascend");
+    rgi_axis_linspace<<<(unsigned)((ntgt + 127) / 128), 128, 0, as_stream(stream)>>>(
+        src_start, src_stop, nsrc, tgt_start, tgt_stop, ntgt, idx, w, oob);
+    DFCSR_LAUNCH_CHECK();
+    return DFCSR_OK;
+}
 
 extern "C" int dfcsr_history_regrid(const double *density, const double *density_x,
                                     const double *density_z, const double *vx, const double *vx_x,

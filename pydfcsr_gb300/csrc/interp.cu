@@ -47,9 +47,38 @@ __global__ void interp1d_kernel(const double *__restrict__ q, int64_t m, const d
     out[i] = __dadd_rn(__dmul_rn(tab[a], __dsub_rn(1.0, f)), __dmul_rn(tab[b], f));
 }
 
+// Observation mesh of get_CSR_mesh (CSR.py:361-394) as the points that
+// calculate_2D_CSR visits (CSR.py:404-415): point k = i * zbins + j,
+// s = position + zrange[j], x = xrange[i] + polyval([slope0, slope1], zrange[j]),
+// with numpy's linspace and polyval arithmetic.
+__global__ void csr_mesh_kernel(double x0, double x1, int xbins, double z0, double z1, int zbins,
+                                double slope0, double slope1, double position,
+                                double *__restrict__ s, double *__restrict__ x) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (int64_t)xbins * zbins) return;
+    const int i = (int)(k / zbins), j = (int)(k % zbins);
+    const double z = np_linspace_at(z0, z1, zbins, j);
+    const double xt = np_linspace_at(x0, x1, xbins, i);
+    s[k] = __dadd_rn(position, z);
+    x[k] = __dadd_rn(xt, __dadd_rn(__dmul_rn(slope0, z), slope1));
+}
+
 }  // namespace dfcsr
 
 using namespace dfcsr;
+
+extern "C" int dfcsr_csr_mesh(double x0, double x1, int xbins, double z0, double z1, int zbins,
+                              double slope0, double slope1, double position, double *s, double *x,
+                              void *stream) {
+    clear_error();
+    DFCSR_CHECK_ARG(xbins >= 1 && zbins >= 1, "dfcsr_csr_mesh: empty mesh (%d x %d)", xbins, zbins);
+    DFCSR_CHECK_ARG(s && x, "dfcsr_csr_mesh: null pointer");
+    const int64_t n = (int64_t)xbins * zbins;
+    csr_mesh_kernel<<<(unsigned)((n + 255) / 256), 256, 0, as_stream(stream)>>>(
+        x0, x1, xbins, z0, z1, zbins, slope0, slope1, position, s, x);
+    DFCSR_LAUNCH_CHECK();
+    return DFCSR_OK;
+}
 
 extern "C" int dfcsr_interp3d(const double *qt, const double *qx, const double *qz, int64_t m,
                               const double *data, int nt, int nx, int nz, double min_t, double min_x,

@@ -25,7 +25,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .coeffs import gradient_table, rgi_axis, savgol_tables
+from .coeffs import gradient_table, savgol_tables
 from .runtime import (as_device_f64, default_workspace, host_to_device, ptr, require_cuda,
                       stream_handle)
 
@@ -51,18 +51,21 @@ def beam_moments(x, z, stream=None, ws=None):
 
 
 def deposit_cic(q1, q2, w0, w1, nbins_1, bins_start_1, bins_end_1, nbins_2, bins_start_2,
-                bins_end_2, stream=None, ws=None):
+                bins_end_2, stream=None, ws=None, out0=None, out1=None):
     """Deterministic CIC deposit of up to two weight channels (device tensors).
 
     ``w0 = None`` deposits unit weights.  Returns (out0, out1 or None), each a
-    float64 CUDA tensor of shape (nbins_1, nbins_2).
+    float64 CUDA tensor of shape (nbins_1, nbins_2) (written into ``out0`` /
+    ``out1`` when given: contiguous float64 of that many elements).
     """
     require_cuda()
     n = q1.numel()
     ws = ws or default_workspace()
     nb1, nb2 = int(nbins_1), int(nbins_2)
-    out0 = torch.empty((nb1, nb2), dtype=torch.float64, device=q1.device)
-    out1 = torch.empty((nb1, nb2), dtype=torch.float64, device=q1.device) if w1 is not None else None
+    if out0 is None:
+        out0 = torch.empty((nb1, nb2), dtype=torch.float64, device=q1.device)
+    if out1 is None and w1 is not None:
+        out1 = torch.empty((nb1, nb2), dtype=torch.float64, device=q1.device)
     need = _lib.query("dfcsr_deposit_workspace_bytes", n, nb1, nb2)
     buf = ws.get("deposit", need)
     _lib.call("dfcsr_deposit_cic2d", ptr(q1), ptr(q2), ptr(w0), ptr(w1), n, nb1,
@@ -163,10 +166,14 @@ class HistoryRing:
 
 
 class _DFEntry:
-    __slots__ = ("x_grids", "z_grids", "fields", "scalars", "t", "sigma_x", "sigma_z")
+    """One logged DF: grids (numpy linspaces and their (start, stop, n)),
+    the five fields on the device, the finalisation scalars, t and sigmas."""
+    __slots__ = ("x_grids", "z_grids", "x_lin", "z_lin", "fields", "scalars", "t", "sigma_x",
+                 "sigma_z")
 
-    def __init__(self, x_grids, z_grids, fields, scalars, t, sigma_x, sigma_z):
+    def __init__(self, x_grids, z_grids, fields, scalars, t, sigma_x, sigma_z, x_lin, z_lin):
         self.x_grids, self.z_grids = x_grids, z_grids
+        self.x_lin, self.z_lin = x_lin, z_lin
         self.fields, self.scalars = fields, scalars
         self.t, self.sigma_x, self.sigma_z = t, sigma_x, sigma_z
 
@@ -257,14 +264,13 @@ class DF_tracker:
         z1 = self.zmean + self.zlim * sigma_z
         xg = np.linspace(x0, x1, xb)
         zg = np.linspace(z0, z1, zb)
-        density, vxsum = deposit_cic(xd, zd, None, pxd, xb, x0, x1, zb, z0, z1, stream, ws)
         fields = torch.empty((5, xb, zb), dtype=torch.float64, device=xd.device)
-        fields[0].copy_(density)
-        fields[3].copy_(vxsum)
-        sc = torch.zeros(8, dtype=torch.float64, device=xd.device)
+        deposit_cic(xd, zd, None, pxd, xb, x0, x1, zb, z0, z1, stream, ws, out0=fields[0],
+                    out1=fields[3])
+        sc = torch.empty(8, dtype=torch.float64, device=xd.device)   # written by df_finalize
         self._finalize(fields, sc, xg, zg, win, stream, ws)
         self.x_grids, self.z_grids = xg, zg
-        self._cur = _DFEntry(xg, zg, fields, sc, t, sigma_x, sigma_z)
+        self._cur = _DFEntry(xg, zg, fields, sc, t, sigma_x, sigma_z, (x0, x1, xb), (z0, z1, zb))
         self.t = t
         self.bins = (xb, zb, win)
 
@@ -338,31 +344,24 @@ class DF_tracker:
         self.end_time = self.time_log[-1]
 
     def _regrid_into_ring(self, entry, stream=None):
-        ix, wx, ox = rgi_axis(entry.x_grids, self.x_grid_interp)
-        iz, wz, oz = rgi_axis(entry.z_grids, self.z_grid_interp)
-        nxi, nzi = ix.size, iz.size
-        # pack the index tables into one copy: int32 idx | f64 w | u8 oob
-        blob = np.zeros(13 * (nxi + nzi) + 6 * 16 + 32, dtype=np.uint8)
-        o = 0
-        views = []
-        for arr in (wx, wz, ix, iz, ox, oz):
-            b = np.ascontiguousarray(arr).view(np.uint8)
-            blob[o:o + b.size] = b
-            views.append(o)
-            o += (b.size + 15) // 16 * 16
-        dev = host_to_device(blob[:o + 16])
-        base = dev.data_ptr()
+        """Regrid one logged DF into a new ring slot: axis tables on the
+        device (both grids are linspaces), then the five-field regrid."""
+        (xs0, xs1, xsn), (zs0, zs1, zsn) = entry.x_lin, entry.z_lin
+        (xt0, xt1, nxi), (zt0, zt1, nzi) = self.x_interp_lin, self.z_interp_lin
+        pad = lambda b: (b + 255) // 256 * 256
+        sizes = [pad(8 * nxi), pad(8 * nzi), pad(4 * nxi), pad(4 * nzi), pad(nxi), pad(nzi)]
+        buf = self._workspace().get("rgi", sum(sizes))
+        offs = np.concatenate([[0], np.cumsum(sizes)])
+        wx, wz, ix, iz, ox, oz = (ctypes.c_void_p(buf.data_ptr() + int(o)) for o in offs[:6])
+        h = stream_handle(stream)
+        _lib.call("dfcsr_rgi_axis_linspace", xs0, xs1, xsn, xt0, xt1, nxi, ix, wx, ox, h)
+        _lib.call("dfcsr_rgi_axis_linspace", zs0, zs1, zsn, zt0, zt1, nzi, iz, wz, oz, h)
         s64, s32 = self.ring.push()
         f = entry.fields
         _lib.call("dfcsr_history_regrid", ptr(f[0]), ptr(f[1]), ptr(f[2]), ptr(f[3]), ptr(f[4]),
-                  f.shape[1], f.shape[2],
-                  ctypes.c_void_p(base + views[2]), ctypes.c_void_p(base + views[0]),
-                  ctypes.c_void_p(base + views[4]), nxi,
-                  ctypes.c_void_p(base + views[3]), ctypes.c_void_p(base + views[1]),
-                  ctypes.c_void_p(base + views[5]), nzi,
+                  f.shape[1], f.shape[2], ix, wx, ox, nxi, iz, wz, oz, nzi,
                   ctypes.c_void_p(entry.scalars.data_ptr() + 8 * 4),
-                  ptr(s64), ptr(s32), stream_handle(stream))
-        self._regrid_blob = dev
+                  ptr(s64), ptr(s32), h)
 
     def _new_ring(self, nxi, nzi):
         store64 = self.precision in ("fp64", "both")
@@ -393,10 +392,12 @@ class DF_tracker:
             zbins = min(zbins, self.upper_limit)
         self.sigma_x_interp = max_sigma_x
         self.sigma_z_interp = max_sigma_z
-        self.x_grid_interp = np.linspace(self.xmean - 5 * self.sigma_x_interp,
-                                         self.xmean + 5 * self.sigma_x_interp, xbins)
-        self.z_grid_interp = np.linspace(self.zmean - 5 * self.sigma_z_interp,
-                                         self.zmean + 5 * self.sigma_z_interp, zbins)
+        self.x_interp_lin = (self.xmean - 5 * self.sigma_x_interp,
+                             self.xmean + 5 * self.sigma_x_interp, xbins)
+        self.z_interp_lin = (self.zmean - 5 * self.sigma_z_interp,
+                             self.zmean + 5 * self.sigma_z_interp, zbins)
+        self.x_grid_interp = np.linspace(*self.x_interp_lin)
+        self.z_grid_interp = np.linspace(*self.z_interp_lin)
         self._new_ring(xbins, zbins)
         self.time_interp = self.time_log.copy()
         for entry in self.DF_log:

@@ -166,6 +166,10 @@ def test_wake_fp64_golden(tag):
     csr.get_CSR_mesh()
     np.testing.assert_allclose(csr.CSR_xmesh, g["xmesh"], rtol=1e-12, atol=1e-18)
     np.testing.assert_allclose(csr.CSR_zmesh, g["zmesh"], rtol=1e-12, atol=1e-18)
+    # the device mesh is the host mesh bit for bit
+    sd, xd = csr.mesh_device()
+    assert np.array_equal(sd.cpu().numpy(), run.beam.position + csr.CSR_zmesh)
+    assert np.array_equal(xd.cpu().numpy(), csr.CSR_xmesh)
     s = run.beam.position + g["zmesh"][g["points"]]
     x = g["xmesh"][g["points"]]
     dE, xk = csr.wake_device(torch.from_numpy(s).cuda(), torch.from_numpy(x).cuda(), "fp64")
@@ -257,3 +261,29 @@ def test_wake_chicane_mixed_vs_oracle():
     e = wake_errors(dE32, xk32, ref[0], ref[1])
     assert e["max_rel"] < 1e-4 and e["rms_rel"] < 1e-4, e
     assert e["pointwise_dE"] < 1e-2 and e["pointwise_xk"] < 1e-2, e
+
+
+@cuda
+def test_rgi_axis_tables_on_device_equal_host():
+    """dfcsr_rgi_axis_linspace == the RegularGridInterpolator tables computed
+    from the numpy linspace arrays (bit for bit), including targets outside
+    the source grid on both sides and targets on source points."""
+    import ctypes
+    from pydfcsr_gb300 import _lib
+    from pydfcsr_gb300.coeffs import rgi_axis
+    from pydfcsr_gb300.runtime import ptr, stream_handle
+    cases = [((-1.0e-4, 1.0e-4, 256), (-1.3e-4, 1.3e-4, 500)),
+             ((2.0, 3.0, 11), (2.0, 3.0, 11)),
+             ((2.0, 3.0, 11), (2.0, 3.0, 21)),
+             ((-5e-5, 7e-5, 128), (-2e-5, 2e-5, 600)),
+             ((0.0, 1.0, 2), (-0.5, 1.5, 9))]
+    for (s0, s1, ns), (t0, t1, nt) in cases:
+        i_ref, w_ref, o_ref = rgi_axis(np.linspace(s0, s1, ns), np.linspace(t0, t1, nt))
+        idx = torch.empty(nt, dtype=torch.int32, device="cuda")
+        w = torch.empty(nt, dtype=torch.float64, device="cuda")
+        o = torch.empty(nt, dtype=torch.uint8, device="cuda")
+        _lib.call("dfcsr_rgi_axis_linspace", s0, s1, ns, t0, t1, nt, ptr(idx), ptr(w), ptr(o),
+                  stream_handle())
+        assert np.array_equal(idx.cpu().numpy(), i_ref)
+        assert np.array_equal(w.cpu().numpy(), w_ref)
+        assert np.array_equal(o.cpu().numpy(), o_ref)
