@@ -158,9 +158,14 @@ def device_step_sets(run, steps):
     return sets
 
 
-def timed_steps(run, sets, first, count, precision, events=None, wake=True):
+def timed_steps(run, sets, first, count, precision, events=None, wake=True, side=None):
     """Run steps first..first+count-1 from device-resident particle sets;
-    ``events`` (list) receives one (start, end) CUDA event pair per step."""
+    ``events`` (list) receives one (start, end) CUDA event pair per step.
+
+    ``side``: a second stream for the beam moments.  The particle sets are
+    resident before the loop, so the moments of step k+1 need not wait for
+    the wake of step k on the main stream: the host gets them while the GPU
+    is still busy and enqueues step k+1 behind the wake without a gap."""
     import torch
     csr = run.csr
     stream = torch.cuda.current_stream()
@@ -169,7 +174,7 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True):
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record(stream)
         run.beam.particle = sets[k - 1]
-        run.beam.update_status()
+        run.beam.update_status(stream=side)
         run.beam.position = float(run.plan.positions[k])
         run.beam.step = k
         lf = run.plan.formation_length(k, run.beam.sigma_z)
@@ -183,25 +188,45 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True):
             events.append(ev)
 
 
-def e2e_steps(run, host_sets, first, count, precision, dev_buf):
+def e2e_steps(run, host_sets, first, count, precision, dev_bufs, side):
     """Steps through the public API with host buffers: H2D of (x, px, z)
-    from pinned memory, CSR2D calls, D2H of (dE_dct, x_kick)."""
+    from pinned memory, CSR2D calls, D2H of (dE_dct, x_kick).
+
+    Pipelined like a caller that streams beams through: step k+1's upload and
+    moments run on ``side`` into the other of two device buffers while step
+    k's wake runs on the main stream, and step k's results (calculate_2D_CSR
+    with wait=False) are read back after step k+1 is enqueued."""
+    import torch
     csr = run.csr
+    main = torch.cuda.current_stream()
     h2d = d2h = 0
+    used = [None, None]           # event: last read of each device buffer (get_DF)
+    pending = None
     for k in range(first, first + count):
         xpz = host_sets[k - 1]                      # pinned (3, N): x, px, z
-        dev_buf[0].copy_(xpz[0], non_blocking=True)
-        dev_buf[1].copy_(xpz[1], non_blocking=True)
-        dev_buf[4].copy_(xpz[2], non_blocking=True)
+        buf = dev_bufs[k % 2]
+        with torch.cuda.stream(side):
+            if used[k % 2] is not None:
+                side.wait_event(used[k % 2])
+            buf[0].copy_(xpz[0], non_blocking=True)
+            buf[1].copy_(xpz[1], non_blocking=True)
+            buf[4].copy_(xpz[2], non_blocking=True)
         h2d += xpz.numel() * 8
-        run.beam.particle = dev_buf
-        run.beam.update_status()
+        run.beam.particle = buf
+        run.beam.update_status(stream=side)
+        main.wait_event(side.record_event())
         run.beam.position = float(run.plan.positions[k])
         lf = run.plan.formation_length(k, run.beam.sigma_z)
         csr.update_history(lf)
+        used[k % 2] = main.record_event()
         csr.get_CSR_mesh()
-        csr.calculate_2D_CSR(precision)             # reads dE_dct, x_kick back to the host
-        d2h += csr.dE_dct.nbytes + csr.x_kick.nbytes
+        nxt = csr.calculate_2D_CSR(precision, wait=False)
+        if pending is not None:
+            dE, xk = pending.result()               # step k-1 on the host
+            d2h += dE.nbytes + xk.nbytes
+        pending = nxt
+    dE, xk = pending.result()
+    d2h += dE.nbytes + xk.nbytes
     return h2d // count, d2h // count
 
 
@@ -228,7 +253,8 @@ def gpu_arm(a):
         torch.cuda.synchronize()
 
     # warm-up (builds the history; untimed)
-    timed_steps(run, sets, 1, W, a.precision)
+    side = torch.cuda.Stream()
+    timed_steps(run, sets, 1, W, a.precision, side=side)
     barrier()
     fma_peaks = measure_fma_peaks()
     barrier()
@@ -242,7 +268,7 @@ def gpu_arm(a):
     t0 = time.perf_counter()
     step_events = []
     e0.record(stream)
-    timed_steps(run, sets, W + 1, K, a.precision, events=step_events)
+    timed_steps(run, sets, W + 1, K, a.precision, events=step_events, side=side)
     e1.record(stream)
     barrier()
     wall = time.perf_counter() - t0
@@ -314,12 +340,12 @@ def gpu_arm(a):
     if not a.no_fp64 and a.precision == "mixed":
         r64, _ = make_run(wl, lattice, "fp64", seed_offset=rank)
         K64 = min(K, 3)
-        timed_steps(r64, sets, 1, W + K - K64 - 1, "fp64", wake=False)
-        timed_steps(r64, sets, W + K - K64, 1, "fp64")          # warm the FP64 kernel
+        timed_steps(r64, sets, 1, W + K - K64 - 1, "fp64", wake=False, side=side)
+        timed_steps(r64, sets, W + K - K64, 1, "fp64", side=side)   # warm the FP64 kernel
         torch.cuda.synchronize()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record(stream)
-        timed_steps(r64, sets, W + K - K64 + 1, K64, "fp64")
+        timed_steps(r64, sets, W + K - K64 + 1, K64, "fp64", side=side)
         f1.record(stream)
         torch.cuda.synchronize()
         ms64 = f0.elapsed_time(f1) / K64
@@ -343,11 +369,11 @@ def gpu_arm(a):
             h = torch.empty((3, t.shape[1]), dtype=torch.float64, pin_memory=True)
             h.copy_(t[[0, 1, 4]])
             host_sets.append(h)
-        dev_buf = torch.zeros_like(sets[0])
-        e2e_steps(re2e, host_sets, 1, W, a.precision, dev_buf)
+        dev_bufs = [torch.zeros_like(sets[0]), torch.zeros_like(sets[0])]
+        e2e_steps(re2e, host_sets, 1, W, a.precision, dev_bufs, side)
         barrier()
         g0 = time.perf_counter()
-        h2d, d2h = e2e_steps(re2e, host_sets, W + 1, K, a.precision, dev_buf)
+        h2d, d2h = e2e_steps(re2e, host_sets, W + 1, K, a.precision, dev_bufs, side)
         barrier()
         e2e_s = time.perf_counter() - g0
         out["e2e"] = {"value": world * npts * K / e2e_s, "unit": UNIT,

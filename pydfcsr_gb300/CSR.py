@@ -29,7 +29,7 @@ from .lattice import Lattice
 from .params import CSR_params, Integration_params
 from .runtime import as_device_f64, default_workspace, ptr, require_cuda, stream_handle
 
-__all__ = ["CSR2D", "WakeEvaluator"]
+__all__ = ["CSR2D", "WakeEvaluator", "PendingWake"]
 
 
 def wake_job(tracker, lattice, position, sigma_z, sigma_x, slope0, mean_x, formation_length,
@@ -100,6 +100,29 @@ class WakeEvaluator:
         return dE, xk
 
 
+class PendingWake:
+    """Mesh wake whose device->host copy is in flight: ``result()`` waits for
+    it and returns (dE_dct, x_kick) as numpy arrays of ``shape``."""
+
+    def __init__(self, dE, xk, shape):
+        n = dE.numel()
+        self._host = torch.empty((2, n), dtype=torch.float64, pin_memory=True)
+        self._host[0].copy_(dE, non_blocking=True)
+        self._host[1].copy_(xk, non_blocking=True)
+        self._event = torch.cuda.Event()
+        self._event.record()
+        self.shape = shape
+        self.nbytes = 2 * n * 8
+
+    def done(self):
+        return self._event.query()
+
+    def result(self):
+        self._event.synchronize()
+        h = self._host.numpy()
+        return h[0].reshape(self.shape).copy(), h[1].reshape(self.shape).copy()
+
+
 class CSR2D:
     """The CSR wake computation of one beam, on the GPU."""
 
@@ -126,6 +149,8 @@ class CSR2D:
         self._jobs_dev = None
         self._mesh = None
         self._mesh_host = None
+        self._pending = None
+        self._dE_dct = self._x_kick = None
         if beam is not None:
             self.initialization()
 
@@ -236,13 +261,46 @@ class CSR2D:
         return self.evaluator.mixed(jobs, s, x, ip.xbins, ip.zbins,
                                     use_band=self.near_band > 0, stream=stream)
 
-    def calculate_2D_CSR(self, precision=None):
-        """Wake on the whole observation mesh (CSR.py:397-418)."""
+    def calculate_2D_CSR(self, precision=None, wait=True):
+        """Wake on the whole observation mesh (CSR.py:397-418): sets
+        ``dE_dct`` and ``x_kick`` (numpy [xbins, zbins]).
+
+        ``wait=False`` (extension) returns at once with a :class:`PendingWake`;
+        the results are copied to pinned host memory on the stream and
+        ``dE_dct`` / ``x_kick`` wait for that copy when first read."""
         s, x = self.mesh_device()
         dE, xk = self.wake_device(s, x, precision)
         shape = (self.CSR_params.xbins, self.CSR_params.zbins)
-        self.dE_dct = dE.cpu().numpy().reshape(shape)
-        self.x_kick = xk.cpu().numpy().reshape(shape)
+        pending = PendingWake(dE, xk, shape)
+        self._pending = pending
+        if wait:
+            self._resolve()
+            return None
+        return pending
+
+    def _resolve(self):
+        if self._pending is not None:
+            self._dE_dct, self._x_kick = self._pending.result()
+            self._pending = None
+
+    def _get_dE(self):
+        self._resolve()
+        return self._dE_dct
+
+    def _set_dE(self, v):
+        self._pending = None
+        self._dE_dct = v
+
+    def _get_xk(self):
+        self._resolve()
+        return self._x_kick
+
+    def _set_xk(self, v):
+        self._pending = None
+        self._x_kick = v
+
+    dE_dct = property(_get_dE, _set_dE)
+    x_kick = property(_get_xk, _set_xk)
 
     def calculate_2D_CSR_parallel(self, precision=None):
         """One GPU evaluates every observation point: same as calculate_2D_CSR

@@ -52,10 +52,17 @@ class Beam:
             self.particle = self.particle.clone()
             self._owned = True
 
-    def update_status(self):
-        m = beam_moments(self.particle[0], self.particle[4], ws=self.ws)
+    def update_status(self, stream=None):
+        """Beam statistics from one device moments call; waits for it (and
+        for whatever precedes it on ``stream``, default the current one)."""
+        if stream is not None:
+            with torch.cuda.stream(stream):
+                m = beam_moments(self.particle[0], self.particle[4], ws=self.ws)
+                st = m.cpu().numpy()
+        else:
+            m = beam_moments(self.particle[0], self.particle[4], ws=self.ws)
+            st = m.cpu().numpy()
         self._moments_dev = m
-        st = m.cpu().numpy()
         self._moments = st
         self._mean_x, self._mean_z = float(st[1]), float(st[2])
         self._sigma_x, self._sigma_z = float(st[3]), float(st[4])

@@ -287,3 +287,20 @@ def test_rgi_axis_tables_on_device_equal_host():
         assert np.array_equal(idx.cpu().numpy(), i_ref)
         assert np.array_equal(w.cpu().numpy(), w_ref)
         assert np.array_equal(o.cpu().numpy(), o_ref)
+
+
+@cuda
+def test_calculate_2d_csr_nonblocking_matches_blocking():
+    """calculate_2D_CSR(wait=False) gives the same arrays as the blocking call,
+    through the returned handle and through the dE_dct / x_kick attributes."""
+    g = golden("wake_dipole.npz")
+    run = _device_run_from_fixture(g, precision="both")
+    csr = run.csr
+    csr.get_CSR_mesh()
+    csr.calculate_2D_CSR("mixed")
+    dE0, xk0 = csr.dE_dct.copy(), csr.x_kick.copy()
+    pend = csr.calculate_2D_CSR("mixed", wait=False)
+    dE1, xk1 = pend.result()
+    assert np.array_equal(dE0, dE1) and np.array_equal(xk0, xk1)
+    csr.calculate_2D_CSR("mixed", wait=False)
+    assert np.array_equal(csr.dE_dct, dE0) and np.array_equal(csr.x_kick, xk0)
