@@ -334,70 +334,82 @@ struct RingView {
 };
 
 // Integrand contribution of rows [i_lo, i_hi) x columns [0, C) of a chunk.
+// Work unit = one s' column x MX_ROWBLK consecutive x' rows: a warp covers
+// consecutive columns of one row block, so its gathers stay close in the
+// history (neighbouring s' -> neighbouring cells) and the row records it
+// reads are the same for all lanes (shared-memory broadcast); each thread
+// keeps its column record in registers for the rows of its unit.
+constexpr int MX_ROWBLK = 4;
+
 template <bool FF>
 __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const RingView &V, int i_lo,
                                              int i_hi, int C, float &sz, float &cz, float &sx,
                                              float &cx) {
-    const int total = (i_hi - i_lo) * C;
+    const int nblk = (i_hi - i_lo + MX_ROWBLK - 1) / MX_ROWBLK;
+    const int units = nblk * C;
     const int tid = threadIdx.x;
-    // (i, jl) of p = tid + k * MX_THREADS, advanced without integer division
-    int i = tid / C, jl = tid - (tid / C) * C;
-    const int di = MX_THREADS / C, dj = MX_THREADS - (MX_THREADS / C) * C;
+    // (row block, column) of u = tid + k * MX_THREADS, advanced without division
+    int rb = tid / C, jl = tid - (tid / C) * C;
+    const int drb = MX_THREADS / C, dj = MX_THREADS - (MX_THREADS / C) * C;
     const uint32_t nzc = (uint32_t)V.nz * 2u;   // float4 per x row of a slot
-    for (int p = tid; p < total; p += MX_THREADS) {
+    for (int u = tid; u < units; u += MX_THREADS) {
         const float4 *cr = sm.col + jl * (CW / 4);
-        const float4 *rr = sm.row + (i_lo + i) * (RW / 4);
-        const float4 q0 = cr[0], q5 = cr[5];
-        const float4 ra = rr[0];
-        const float4 rw = rr[1];
-        const float wx = rw.x;
-        const float ws = q5.w;
-        i += di;
+        const int i0 = i_lo + rb * MX_ROWBLK;
+        rb += drb;
         jl += dj;
-        if (jl >= C) { jl -= C; i += 1; }
-        if (ws == 0.f || wx == 0.f) continue;
-        const float4 g1 = cr[1];
-        const float u = ra.z;
-        const float r0 = g1.x;
-        const float Dd = u * ((g1.z + 1.f) * u - 2.f * g1.y);
-        const float rad = fmaf(r0, r0, Dd);
-        const float delta = __fdividef(Dd, r0 + rad * rsqrtf(rad));
-        int t0, t1, z0, z1;
-        float td, zd;
-        if (!axis_split(__float_as_int(q0.x), q0.z - delta * V.inv_dt, V.nt, t0, t1, td) ||
-            !axis_split(__float_as_int(q0.y), q0.w + delta * V.inv_dz, V.nz, z0, z1, zd))
-            continue;   // every field is zero outside the history grid
-        // x: rows outside the history grid are not in [i_lo, i_hi)
-        const int x0 = __float_as_int(ra.x);
-        const float xd = ra.y;
-        int s0 = V.head + t0, s1 = V.head + t1;
-        if (s0 >= V.cap) s0 -= V.cap;
-        if (s1 >= V.cap) s1 -= V.cap;
-        const uint32_t c0x0 = ((uint32_t)s0 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
-        const uint32_t c1x0 = ((uint32_t)s1 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
-        const uint32_t dxc = (uint32_t)__float_as_int(rw.y) * nzc;
-        const Fields5 F = gather5<FF>(V.ring, c0x0, c1x0, c0x0 + dxc, c1x0 + dxc,
-                                      2u * (uint32_t)(z1 - z0), td, xd, zd);
-        const float4 q2 = cr[2], q3 = cr[3], q4 = cr[4];
-        const float inv_r = __fdividef(1.f, r0 + delta);
-        const float scale = fmaf(ra.w, g1.w, 1.f);
-        const float vr = F.vx;
-        // brx = (K0x - vx') - vx' (K1x - 1 + vx' K2x); brz = K0z - vx' (K1z + vx' K2z)
-        const float brx = (q3.y - vr) - vr * fmaf(vr, q3.w, q3.z);
-        const float brz = q4.x - vr * fmaf(vr, q4.z, q4.y);
-        const float p1 = fmaf(vr, q2.y, q2.x);
-        const float num = scale * F.dx * brx + F.dz * brz - scale * p1 * F.den * F.vxx;
-        const float Iz = num * inv_r;
-        const float Q1 = q5.x;
-        const float q1 = q4.w - u * Q1;
-        const float M = q5.z - u * Q1 - q5.y * delta;
-        const float e = q2.z;
-        const float pd = -(F.dx * fmaf(vr, q2.w, e) + F.dz * __fdividef(fmaf(vr, e, q3.x), scale)) -
-                         F.den * F.vxx;
-        const float Ix = scale * inv_r * inv_r * (q1 * inv_r * F.den + pd * M);
-        const float w = wx * ws;
-        kahan(sz, cz, w * Iz);
-        kahan(sx, cx, w * Ix);
+        if (jl >= C) { jl -= C; rb += 1; }
+        const float4 q0 = cr[0], q5 = cr[5];
+        const float ws = q5.w;
+        if (ws == 0.f) continue;
+        const float4 g1 = cr[1], q2 = cr[2], q3 = cr[3], q4 = cr[4];
+        const int iend = min(i0 + MX_ROWBLK, i_hi);
+        for (int i = i0; i < iend; ++i) {
+            const float4 *rr = sm.row + i * (RW / 4);
+            const float4 ra = rr[0];
+            const float4 rw = rr[1];
+            const float wx = rw.x;
+            if (wx == 0.f) continue;
+            const float u = ra.z;
+            const float r0 = g1.x;
+            const float Dd = u * ((g1.z + 1.f) * u - 2.f * g1.y);
+            const float rad = fmaf(r0, r0, Dd);
+            const float delta = __fdividef(Dd, r0 + rad * rsqrtf(rad));
+            int t0, t1, z0, z1;
+            float td, zd;
+            if (!axis_split(__float_as_int(q0.x), q0.z - delta * V.inv_dt, V.nt, t0, t1, td) ||
+                !axis_split(__float_as_int(q0.y), q0.w + delta * V.inv_dz, V.nz, z0, z1, zd))
+                continue;   // every field is zero outside the history grid
+            // x: rows outside the history grid are not in [i_lo, i_hi)
+            const int x0 = __float_as_int(ra.x);
+            const float xd = ra.y;
+            int s0 = V.head + t0, s1 = V.head + t1;
+            if (s0 >= V.cap) s0 -= V.cap;
+            if (s1 >= V.cap) s1 -= V.cap;
+            const uint32_t c0x0 = ((uint32_t)s0 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
+            const uint32_t c1x0 = ((uint32_t)s1 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
+            const uint32_t dxc = (uint32_t)__float_as_int(rw.y) * nzc;
+            const Fields5 F = gather5<FF>(V.ring, c0x0, c1x0, c0x0 + dxc, c1x0 + dxc,
+                                          2u * (uint32_t)(z1 - z0), td, xd, zd);
+            const float inv_r = __fdividef(1.f, r0 + delta);
+            const float scale = fmaf(ra.w, g1.w, 1.f);
+            const float vr = F.vx;
+            // brx = (K0x - vx') - vx' (K1x - 1 + vx' K2x); brz = K0z - vx' (K1z + vx' K2z)
+            const float brx = (q3.y - vr) - vr * fmaf(vr, q3.w, q3.z);
+            const float brz = q4.x - vr * fmaf(vr, q4.z, q4.y);
+            const float p1 = fmaf(vr, q2.y, q2.x);
+            const float num = scale * F.dx * brx + F.dz * brz - scale * p1 * F.den * F.vxx;
+            const float Iz = num * inv_r;
+            const float Q1 = q5.x;
+            const float q1 = q4.w - u * Q1;
+            const float M = q5.z - u * Q1 - q5.y * delta;
+            const float e = q2.z;
+            const float pd = -(F.dx * fmaf(vr, q2.w, e) + F.dz * __fdividef(fmaf(vr, e, q3.x), scale)) -
+                             F.den * F.vxx;
+            const float Ix = scale * inv_r * inv_r * (q1 * inv_r * F.den + pd * M);
+            const float w = wx * ws;
+            kahan(sz, cz, w * Iz);
+            kahan(sx, cx, w * Ix);
+        }
     }
 }
 
