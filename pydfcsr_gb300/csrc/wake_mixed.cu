@@ -63,7 +63,61 @@ __host__ __device__ inline size_t point_record_words(int xbins, int zbins) {
     return (size_t)WAKE_MAX_REGIONS * zbins * CW + (size_t)5 * xbins * RW;
 }
 
-__device__ __forceinline__ int clamp_int(double v) { return (int)fmax(fmin(v, 2.0e9), -2.0e9); }
+// The geometry kernel is bound by the FP64 pipe, which also executes FP64
+// conversions and comparisons.  These helpers move such work to the integer
+// pipe.
+//
+// FP64 -> FP32 with round-to-nearest-even from the bit patterns (IEEE 754:
+// keep the top 23 of 52 mantissa bits, round on the 29 dropped bits; a carry
+// out of the mantissa steps the exponent, up to infinity).  Zeros are exact;
+// subnormal, overflowing and non-finite inputs (not produced by the geometry)
+// take the hardware conversion.
+__device__ __forceinline__ float d2f(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    if ((b << 1) == 0ull) return __uint_as_float(sign);
+    const int e32 = (int)((b >> 52) & 0x7ffu) - 1023 + 127;
+    if (e32 < 1 || e32 > 254) return __double2float_rn(v);
+    const unsigned long long m = b & 0xfffffffffffffull;
+    const unsigned int mm = (unsigned int)(m >> 29), rem = (unsigned int)(m & 0x1fffffffu);
+    unsigned int bits = sign | ((unsigned int)e32 << 23) | mm;
+    if (rem > 0x10000000u || (rem == 0x10000000u && (mm & 1u))) bits += 1u;
+    return __uint_as_float(bits);
+}
+
+// Signed 64-bit key with the order of the doubles (non-NaN; -0 as +0).
+__device__ __forceinline__ long long order_key(double v) {
+    long long b = __double_as_longlong(v);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+
+// rho_at (curvature of the element containing s', CSR.py:651-656) with the
+// element-boundary comparisons done on order keys.
+__device__ __forceinline__ float rho_at_key(const dfcsr_wake_job &J, long long spk) {
+    double r = 0.0;
+    long long prev = 0;
+    for (int e = 0; e < J.nelement; ++e) {
+        const long long dk = order_key(J.distance[e]);
+        if (e == 0) {
+            if (spk < dk) r = J.rho[0];
+        } else if (spk < dk && spk >= prev) {
+            r = J.rho[e];
+        }
+        prev = dk;
+    }
+    return d2f(r);
+}
+
+// Integer cell (clamped to +-2e9, NaN -> 2e9: outside every grid) and FP32
+// offset in [0, 1) of a history coordinate.
+__device__ __forceinline__ void cell_split(double u, int &cell, float &off) {
+    const double fl = floor(u);
+    off = d2f(u - fl);
+    const int c = __double2int_rz(fl);   // fl is integral; saturates for huge |u|
+    const bool nan = (__double_as_longlong(u) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+    cell = nan ? 2000000000 : max(min(c, 2000000000), -2000000000);
+}
 
 // s' of column j and x' of row i: start + k * step (the reference's
 // linspace up to rounding, which the mixed path does not need to reproduce).
@@ -129,7 +183,13 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
     if (b >= count) return;
     const dfcsr_wake_job &J = jobs[job_of_point ? job_of_point[pt] : 0];
     const double t = J.position, s = S[pt], x = X[pt];
-    if (threadIdx.x == 0) {
+    // the three independent per-point set-up tasks run in three warps
+    if (threadIdx.x == 32) {
+        gs.vx_obs = hist_field_fp64(J, 3, t, x, s - t);
+        obs_vx[b] = gs.vx_obs;
+    } else if (threadIdx.x == 64) {
+        lattice_lerp(J, s, gs.lat_s);
+    } else if (threadIdx.x == 0) {
         gs.nreg = wake_regions(J, s, x, gs.reg);
         bool ok;
         layout(gs.reg, gs.nreg, gs.rm, ok, rec_words);
@@ -140,9 +200,6 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         for (int k = 0; k < WAKE_MAX_REGIONS; ++k)
             m.reg[k] = (k < gs.nreg) ? gs.rm[k] : RegionMeta{0, 0, 0, 0};
         meta[b] = m;
-        gs.vx_obs = hist_field_fp64(J, 3, t, x, s - t);
-        obs_vx[b] = gs.vx_obs;
-        lattice_lerp(J, s, gs.lat_s);
         int cb = 0, rb = 0;
         for (int r = 0; r < gs.nreg; ++r) {
             const Region &R = gs.reg[r];
@@ -195,7 +252,10 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         const double r0 = sqrt(rx0 * rx0 + ry0 * ry0);
         const double ut0 = (t - r0 - J.t_min) * inv_t;
         const double uz0 = (spj - (t - r0) - J.z_min) * inv_z;
-        const double tfl = floor(ut0), zfl = floor(uz0);
+        int tcell, zcell;
+        float toff, zoff;
+        cell_split(ut0, tcell, toff);
+        cell_split(uz0, zcell, zoff);
         const double a = vxo * tpx + vyo * tpy, bb = vxo * npx + vyo * npy;
         const double e = tpx * npx + tpy * npy, g = npx * npx + npy * npy;
         const double h = tpx * tpx + tpy * tpy;
@@ -204,17 +264,14 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         const double q2 = nsx * tpx + nsy * tpy;
         const bool near = J.near_band > 0.0 && fabs(spj - s) < J.near_band;
         float4 *o = reinterpret_cast<float4 *>(prec + gs.rm[r].col_off) + (size_t)j * (CW / 4);
-        o[0] = make_float4(__int_as_float(clamp_int(tfl)), __int_as_float(clamp_int(zfl)),
-                           (float)(ut0 - tfl), (float)(uz0 - zfl));
-        o[1] = make_float4((float)r0, (float)(rx0 * npx + ry0 * npy), (float)(g - 1.0),
-                           (float)rho_at(J, spj));
-        o[2] = make_float4((float)a, (float)bb, (float)e, (float)g);
-        o[3] = make_float4((float)h, (float)(bb - a * e), (float)((a * g - 1.0) + bb * e),
-                           (float)(bb * g));
-        o[4] = make_float4((float)(a * (1.0 - h)), (float)(a * e + bb * h), (float)(bb * e),
-                           (float)Q0);
-        o[5] = make_float4((float)(npx * nmx + npy * nmy), (float)q2, (float)(Q0 - q2 * r0),
-                           near ? 0.f : (float)ax_s.weight(j));   // band columns: FP64 kernel
+        o[0] = make_float4(__int_as_float(tcell), __int_as_float(zcell), toff, zoff);
+        o[1] = make_float4(d2f(r0), d2f(rx0 * npx + ry0 * npy), d2f(g - 1.0),
+                           rho_at_key(J, order_key(spj)));
+        o[2] = make_float4(d2f(a), d2f(bb), d2f(e), d2f(g));
+        o[3] = make_float4(d2f(h), d2f(bb - a * e), d2f((a * g - 1.0) + bb * e), d2f(bb * g));
+        o[4] = make_float4(d2f(a * (1.0 - h)), d2f(a * e + bb * h), d2f(bb * e), d2f(Q0));
+        o[5] = make_float4(d2f(npx * nmx + npy * nmy), d2f(q2), d2f(Q0 - q2 * r0),
+                           near ? 0.f : d2f(ax_s.weight(j)));   // band columns: FP64 kernel
     }
     // rows: x cell, offset, u = x' - x'_ref, x', trapz weight; valid row range
     const int nrows = gs.row_begin[nreg];
@@ -232,8 +289,8 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         double xw = 0.0;
         const bool in = axis_index(ux, J.nx, x0, x1, xw);
         float4 *rb = reinterpret_cast<float4 *>(prec + gs.rm[r].row_off);
-        rb[2 * i] = make_float4(__int_as_float(x0), (float)xw, (float)(xpi - gs.xref[r]), (float)xpi);
-        rb[2 * i + 1] = make_float4((float)ax_x.weight(i), __int_as_float(x1 - x0), 0.f, 0.f);
+        rb[2 * i] = make_float4(__int_as_float(x0), d2f(xw), d2f(xpi - gs.xref[r]), d2f(xpi));
+        rb[2 * i + 1] = make_float4(d2f(ax_x.weight(i)), __int_as_float(x1 - x0), 0.f, 0.f);
         if (in) {
             atomicMin(&gs.lo[r], i);   // integer min / max: order independent
             atomicMax(&gs.hi[r], i);
@@ -272,14 +329,24 @@ template <bool FF>
 __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint32_t c00, uint32_t c01,
                                            uint32_t c10, uint32_t c11, uint32_t dzc, float td, float xd,
                                            float zd) {
-    const float4 A0 = __ldg(ring + c00), a0 = __ldg(ring + c00 + 1);
-    const float4 A1 = __ldg(ring + c00 + dzc), a1 = __ldg(ring + c00 + dzc + 1);
-    const float4 B0 = __ldg(ring + c01), b0 = __ldg(ring + c01 + 1);
-    const float4 B1 = __ldg(ring + c01 + dzc), b1 = __ldg(ring + c01 + dzc + 1);
-    const float4 C0 = __ldg(ring + c10), c0 = __ldg(ring + c10 + 1);
-    const float4 C1 = __ldg(ring + c10 + dzc), c1 = __ldg(ring + c10 + dzc + 1);
-    const float4 D0 = __ldg(ring + c11), d0 = __ldg(ring + c11 + 1);
-    const float4 D1 = __ldg(ring + c11 + dzc), d1 = __ldg(ring + c11 + dzc + 1);
+    // second half of a cell: (vx_x, density_x low part) as one 8-byte load
+    auto hi2 = [&](uint32_t c) { return __ldg(reinterpret_cast<const float2 *>(ring + c + 1)); };
+    const float4 A0 = __ldg(ring + c00);
+    const float2 a0 = hi2(c00);
+    const float4 A1 = __ldg(ring + c00 + dzc);
+    const float2 a1 = hi2(c00 + dzc);
+    const float4 B0 = __ldg(ring + c01);
+    const float2 b0 = hi2(c01);
+    const float4 B1 = __ldg(ring + c01 + dzc);
+    const float2 b1 = hi2(c01 + dzc);
+    const float4 C0 = __ldg(ring + c10);
+    const float2 c0 = hi2(c10);
+    const float4 C1 = __ldg(ring + c10 + dzc);
+    const float2 c1 = hi2(c10 + dzc);
+    const float4 D0 = __ldg(ring + c11);
+    const float2 d0 = hi2(c11);
+    const float4 D1 = __ldg(ring + c11 + dzc);
+    const float2 d1 = hi2(c11 + dzc);
     auto tri = [&](float v00a, float v00b, float v01a, float v01b, float v10a, float v10b,
                    float v11a, float v11b) -> float {
         const float c00_ = lerp1(v00a, v00b, td);
