@@ -223,6 +223,9 @@ typedef struct {
     int zbins, xbins;           /* Integration_params                         */
     double near_band;           /* mixed only: |s' - s| below which the       */
                                 /* integrand runs in FP64 (0 = none)          */
+    const double *lattice_delta;/* mixed only, optional: [nsample][6] row     */
+                                /* differences lattice[k+1] - lattice[k]      */
+                                /* (last row 0), or NULL                      */
 } dfcsr_wake_job;
 
 /* Plain FP64 drop-in: reproduces the reference's IEEE operation order

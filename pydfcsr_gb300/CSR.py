@@ -62,6 +62,7 @@ def wake_job(tracker, lattice, position, sigma_z, sigma_x, slope0, mean_x, forma
     j.csr_scaling = float(csr_scaling)
     j.zbins, j.xbins = int(zbins), int(xbins)
     j.near_band = float(near_band)
+    j.lattice_delta = lattice.device_deltas().data_ptr()
     return j
 
 

@@ -89,6 +89,7 @@ class WakeJob(ctypes.Structure):
         ("csr_scaling", _c_double),
         ("zbins", _c_int), ("xbins", _c_int),
         ("near_band", _c_double),
+        ("lattice_delta", _p),
     ]
 
 

@@ -63,61 +63,7 @@ __host__ __device__ inline size_t point_record_words(int xbins, int zbins) {
     return (size_t)WAKE_MAX_REGIONS * zbins * CW + (size_t)5 * xbins * RW;
 }
 
-// The geometry kernel is bound by the FP64 pipe, which also executes FP64
-// conversions and comparisons.  These helpers move such work to the integer
-// pipe.
-//
-// FP64 -> FP32 with round-to-nearest-even from the bit patterns (IEEE 754:
-// keep the top 23 of 52 mantissa bits, round on the 29 dropped bits; a carry
-// out of the mantissa steps the exponent, up to infinity).  Zeros are exact;
-// subnormal, overflowing and non-finite inputs (not produced by the geometry)
-// take the hardware conversion.
-__device__ __forceinline__ float d2f(double v) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
-    if ((b << 1) == 0ull) return __uint_as_float(sign);
-    const int e32 = (int)((b >> 52) & 0x7ffu) - 1023 + 127;
-    if (e32 < 1 || e32 > 254) return __double2float_rn(v);
-    const unsigned long long m = b & 0xfffffffffffffull;
-    const unsigned int mm = (unsigned int)(m >> 29), rem = (unsigned int)(m & 0x1fffffffu);
-    unsigned int bits = sign | ((unsigned int)e32 << 23) | mm;
-    if (rem > 0x10000000u || (rem == 0x10000000u && (mm & 1u))) bits += 1u;
-    return __uint_as_float(bits);
-}
-
-// Signed 64-bit key with the order of the doubles (non-NaN; -0 as +0).
-__device__ __forceinline__ long long order_key(double v) {
-    long long b = __double_as_longlong(v);
-    if (b == (long long)0x8000000000000000ull) b = 0;
-    return b ^ ((b >> 63) & 0x7fffffffffffffffll);
-}
-
-// rho_at (curvature of the element containing s', CSR.py:651-656) with the
-// element-boundary comparisons done on order keys.
-__device__ __forceinline__ float rho_at_key(const dfcsr_wake_job &J, long long spk) {
-    double r = 0.0;
-    long long prev = 0;
-    for (int e = 0; e < J.nelement; ++e) {
-        const long long dk = order_key(J.distance[e]);
-        if (e == 0) {
-            if (spk < dk) r = J.rho[0];
-        } else if (spk < dk && spk >= prev) {
-            r = J.rho[e];
-        }
-        prev = dk;
-    }
-    return d2f(r);
-}
-
-// Integer cell (clamped to +-2e9, NaN -> 2e9: outside every grid) and FP32
-// offset in [0, 1) of a history coordinate.
-__device__ __forceinline__ void cell_split(double u, int &cell, float &off) {
-    const double fl = floor(u);
-    off = d2f(u - fl);
-    const int c = __double2int_rz(fl);   // fl is integral; saturates for huge |u|
-    const bool nan = (__double_as_longlong(u) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
-    cell = nan ? 2000000000 : max(min(c, 2000000000), -2000000000);
-}
+__device__ __forceinline__ int clamp_int(double v) { return (int)fmax(fmin(v, 2.0e9), -2.0e9); }
 
 // s' of column j and x' of row i: start + k * step (the reference's
 // linspace up to rounding, which the mixed path does not need to reproduce).
@@ -222,9 +168,13 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
     const double vxo = gs.lat_s[4] + gs.vx_obs * nsx, vyo = gs.lat_s[5] + gs.vx_obs * nsy;
     const double inv_s = 1.0 / J.s_delta, inv_t = 1.0 / J.t_delta, inv_z = 1.0 / J.z_delta;
     const double inv_x = 1.0 / J.x_delta;
+    // per-point constants: r(s) + x n(s), t - t_min, t + z_min
+    const double Px = fma(x, nsx, X0s), Py = fma(x, nsy, Y0s);
+    const double T0 = t - J.t_min, Tz = t + J.z_min;
     const int nreg = gs.nreg;
     float *prec = rec + (size_t)b * rec_words;
     const int ncols = gs.col_begin[nreg];
+    const double *dtab = J.lattice_delta;
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
         int r = 0;
         while (r + 1 < nreg && c >= gs.col_begin[r + 1]) ++r;
@@ -232,30 +182,38 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         const Axis ax_s = gs.ax_s[r];
         const double xref = gs.xref[r];
         const double spj = ax_s.at(j);
-        // orbit tables at s' (interpolate1D rule, index by multiplication)
+        // orbit tables at s' (interpolate1D rule: in range iff -1 < u < n,
+        // lower index int(u)), one FMA per table column with the differences
         double L[6];
         {
-            int a0, a1;
-            double f;
-            if (axis_index((spj - J.s_min) * inv_s, J.nsample, a0, a1, f)) {
-                const double *pa = J.lattice + (size_t)a0 * 6, *pb = J.lattice + (size_t)a1 * 6;
+            const double u = fma((double)j, ax_s.step * inv_s, (ax_s.start - J.s_min) * inv_s);
+            const int a0 = __double2int_rz(u);   // truncation, saturating
+            const bool nan = (__double_as_longlong(u) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+            // u in (-1, 0) truncates to 0 (extrapolation, like int()); u <= -1
+            // truncates below 0
+            if (!nan && a0 >= 0 && a0 < J.nsample) {
+                const double f = u - (double)a0;
+                const double *pa = J.lattice + (size_t)a0 * 6;
+                if (dtab) {
+                    const double *da = dtab + (size_t)a0 * 6;
 #pragma unroll
-                for (int k = 0; k < 6; ++k) L[k] = fma(f, pb[k] - pa[k], pa[k]);
+                    for (int k = 0; k < 6; ++k) L[k] = fma(f, da[k], pa[k]);
+                } else {
+                    const double *pb = J.lattice + (size_t)(a0 == J.nsample - 1 ? a0 : a0 + 1) * 6;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) L[k] = fma(f, pb[k] - pa[k], pa[k]);
+                }
             } else {
 #pragma unroll
                 for (int k = 0; k < 6; ++k) L[k] = 0.0;
             }
         }
         const double npx = L[2], npy = L[3], tpx = L[4], tpy = L[5];
-        const double Ax = X0s - L[0] + x * nsx, Ay = Y0s - L[1] + x * nsy;
-        const double rx0 = Ax - xref * npx, ry0 = Ay - xref * npy;
-        const double r0 = sqrt(rx0 * rx0 + ry0 * ry0);
-        const double ut0 = (t - r0 - J.t_min) * inv_t;
-        const double uz0 = (spj - (t - r0) - J.z_min) * inv_z;
-        int tcell, zcell;
-        float toff, zoff;
-        cell_split(ut0, tcell, toff);
-        cell_split(uz0, zcell, zoff);
+        const double rx0 = fma(-xref, npx, Px - L[0]), ry0 = fma(-xref, npy, Py - L[1]);
+        const double r0 = sqrt(fma(rx0, rx0, ry0 * ry0));
+        const double ut0 = (T0 - r0) * inv_t;
+        const double uz0 = ((spj - Tz) + r0) * inv_z;
+        const double tfl = floor(ut0), zfl = floor(uz0);
         const double a = vxo * tpx + vyo * tpy, bb = vxo * npx + vyo * npy;
         const double e = tpx * npx + tpy * npy, g = npx * npx + npy * npy;
         const double h = tpx * tpx + tpy * tpy;
@@ -264,14 +222,17 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         const double q2 = nsx * tpx + nsy * tpy;
         const bool near = J.near_band > 0.0 && fabs(spj - s) < J.near_band;
         float4 *o = reinterpret_cast<float4 *>(prec + gs.rm[r].col_off) + (size_t)j * (CW / 4);
-        o[0] = make_float4(__int_as_float(tcell), __int_as_float(zcell), toff, zoff);
-        o[1] = make_float4(d2f(r0), d2f(rx0 * npx + ry0 * npy), d2f(g - 1.0),
-                           rho_at_key(J, order_key(spj)));
-        o[2] = make_float4(d2f(a), d2f(bb), d2f(e), d2f(g));
-        o[3] = make_float4(d2f(h), d2f(bb - a * e), d2f((a * g - 1.0) + bb * e), d2f(bb * g));
-        o[4] = make_float4(d2f(a * (1.0 - h)), d2f(a * e + bb * h), d2f(bb * e), d2f(Q0));
-        o[5] = make_float4(d2f(npx * nmx + npy * nmy), d2f(q2), d2f(Q0 - q2 * r0),
-                           near ? 0.f : d2f(ax_s.weight(j)));   // band columns: FP64 kernel
+        o[0] = make_float4(__int_as_float(clamp_int(tfl)), __int_as_float(clamp_int(zfl)),
+                           (float)(ut0 - tfl), (float)(uz0 - zfl));
+        o[1] = make_float4((float)r0, (float)(rx0 * npx + ry0 * npy), (float)(g - 1.0),
+                           (float)rho_at(J, spj));
+        o[2] = make_float4((float)a, (float)bb, (float)e, (float)g);
+        o[3] = make_float4((float)h, (float)(bb - a * e), (float)((a * g - 1.0) + bb * e),
+                           (float)(bb * g));
+        o[4] = make_float4((float)(a * (1.0 - h)), (float)(a * e + bb * h), (float)(bb * e),
+                           (float)Q0);
+        o[5] = make_float4((float)(npx * nmx + npy * nmy), (float)q2, (float)(Q0 - q2 * r0),
+                           near ? 0.f : (float)ax_s.weight(j));   // band columns: FP64 kernel
     }
     // rows: x cell, offset, u = x' - x'_ref, x', trapz weight; valid row range
     const int nrows = gs.row_begin[nreg];
@@ -289,8 +250,8 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         double xw = 0.0;
         const bool in = axis_index(ux, J.nx, x0, x1, xw);
         float4 *rb = reinterpret_cast<float4 *>(prec + gs.rm[r].row_off);
-        rb[2 * i] = make_float4(__int_as_float(x0), d2f(xw), d2f(xpi - gs.xref[r]), d2f(xpi));
-        rb[2 * i + 1] = make_float4(d2f(ax_x.weight(i)), __int_as_float(x1 - x0), 0.f, 0.f);
+        rb[2 * i] = make_float4(__int_as_float(x0), (float)xw, (float)(xpi - gs.xref[r]), (float)xpi);
+        rb[2 * i + 1] = make_float4((float)ax_x.weight(i), __int_as_float(x1 - x0), 0.f, 0.f);
         if (in) {
             atomicMin(&gs.lo[r], i);   // integer min / max: order independent
             atomicMax(&gs.hi[r], i);

@@ -132,6 +132,18 @@ class Lattice:
                          torch.from_numpy(np.ascontiguousarray(self.distance)).to(dev))
         return self._dev
 
+    def device_deltas(self):
+        """[Nsample, 6] float64 CUDA tensor of row differences of the table
+        (row k+1 - row k, last row 0), cached: lets a linear interpolation be
+        one fused multiply-add per table column."""
+        if getattr(self, "_dev_delta", None) is None:
+            tab = np.concatenate([self.coords, self.n_vec, self.tau_vec], axis=1)
+            d = np.zeros_like(tab)
+            d[:-1] = tab[1:] - tab[:-1]
+            dev = torch.device("cuda", torch.cuda.current_device())
+            self._dev_delta = torch.from_numpy(np.ascontiguousarray(d)).to(dev)
+        return self._dev_delta
+
 
 def _read_yaml(path):
     try:
