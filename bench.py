@@ -71,6 +71,39 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device):
+    """Max of a per-rank float over all ranks (the slowest rank's time sets
+    the job's time); ``device`` is where the collective's tensor lives
+    ('cuda' under NCCL, 'cpu' under gloo)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(points_per_rank_step, world, step_ms):
+    """Whole-job wake points/s: every rank evaluates its own beam's mesh
+    (weak scaling), timed by the slowest rank."""
+    return world * points_per_rank_step * 1000.0 / step_ms
+
+
+def beam_seed(rank):
+    """Each rank runs an independent beam: the workload's seed offset by rank."""
+    return rank
+
+
+def workload_config(n_particles, precision):
+    return {"workload": "chicane_c2: 4 dipoles 0.5 m +-0.05 rad, drifts 2/0.5/2 m, "
+                        "1 GeV, N=%d, sigma_z 50um, sigma_x 20um, h=-10/m, grid 256x256, "
+                        "SG 9/2, mesh 64x64 every step, 100x100 integration bins" % n_particles,
+            "precision": precision,
+            "l2": "inputs larger than L2: distinct 96 MB particle set per step; history ring "
+                  ">= 190 MB"}
+
+
 def lattice_for(wl, total_steps):
     """The workload's chicane, extended by a drift if more steps are asked."""
     from pydfcsr_gb300.synthetic import StepPlan
@@ -243,7 +276,7 @@ def gpu_arm(a):
     wl = workload(WORKLOAD, n_particles=a.particles)
     W, K = max(a.warmup, 0), a.steps
     lattice = lattice_for(wl, W + K)
-    run, beam0 = make_run(wl, lattice, a.precision, seed_offset=rank)
+    run, beam0 = make_run(wl, lattice, a.precision, seed_offset=beam_seed(rank))
     sets = device_step_sets(run, W + K)
     npts = wl.mesh["xbins"] * wl.mesh["zbins"]
 
@@ -282,24 +315,15 @@ def gpu_arm(a):
     kt = {n: _lib.timing_read(n) for n in names}
     launches = {n: v[1] for n, v in kt.items()}
     kernel_ms = {n: round(v[0] / K, 4) for n, v in kt.items() if v[1]}
-    step_ms = dev_ms / K
-    if world > 1:
-        t = torch.tensor([step_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
-    value = world * npts * 1000.0 / step_ms
+    step_ms = max_over_ranks(dev_ms / K, world, "cuda")
+    value = job_value(npts, world, step_ms)
 
     lat = np.array([ev[0].elapsed_time(ev[1]) for ev in step_events])
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
            "warmup": W, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32+f64" if a.precision == "mixed" else "f64",
            "data": "synthetic (seeded numpy Gaussian beam, r_gen6 transport)",
-           "config": {"workload": "chicane_c2: 4 dipoles 0.5 m +-0.05 rad, drifts 2/0.5/2 m, "
-                                  "1 GeV, N=%d, sigma_z 50um, sigma_x 20um, h=-10/m, grid 256x256, "
-                                  "SG 9/2, mesh 64x64 every step, 100x100 integration bins"
-                                  % run.beam.n_particle,
-                      "precision": a.precision, "l2": "inputs larger than L2: distinct 96 MB "
-                      "particle set per step; history ring >= 190 MB"},
+           "config": workload_config(run.beam.n_particle, a.precision),
            "wall_s_timed": wall, "clocks": ck,
            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "definition": "device time of one full step (DF + history + wake)"}}
@@ -354,7 +378,7 @@ def gpu_arm(a):
 
     # plain FP64 leg on the same steps (for the mixed vs FP64 speed-up)
     if not a.no_fp64 and a.precision == "mixed":
-        r64, _ = make_run(wl, lattice, "fp64", seed_offset=rank)
+        r64, _ = make_run(wl, lattice, "fp64", seed_offset=beam_seed(rank))
         K64 = min(K, 3)
         timed_steps(r64, sets, 1, W + K - K64 - 1, "fp64", wake=False, side=side)
         timed_steps(r64, sets, W + K - K64, 1, "fp64", side=side)   # warm the FP64 kernel
@@ -379,7 +403,7 @@ def gpu_arm(a):
 
     # end to end through the public API with host buffers
     if not a.no_e2e:
-        re2e, _ = make_run(wl, lattice, a.precision, seed_offset=rank)
+        re2e, _ = make_run(wl, lattice, a.precision, seed_offset=beam_seed(rank))
         host_sets = []
         for t in sets[:W + K]:
             h = torch.empty((3, t.shape[1]), dtype=torch.float64, pin_memory=True)
@@ -571,7 +595,7 @@ def reference_arm(a):
            "warmup": min(W, 4), "ms_per_step": sec * 1000, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded numpy Gaussian beam, r_gen6 transport)",
-           "config": {"workload": WORKLOAD, "precision": "fp64 (reference algorithm)"},
+           "config": workload_config(wl.n_particles, "mixed"),
            "impl": "reference",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                             "sample": f"wake on {n_obs} of {npts} mesh points per step, scaled; "
