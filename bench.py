@@ -179,14 +179,18 @@ def make_run(wl, lattice, precision, seed_offset=0):
 
 
 def device_step_sets(run, steps):
-    """Transport on the device once (before timing) and keep every step's
-    particle set resident: list of (6, N) float64 CUDA tensors."""
-    import torch
+    """Transport on the device once (before timing, dfcsr_transport6) and keep
+    every step's particle set resident: list of (6, N) float64 CUDA tensors."""
+    import ctypes
+    from pydfcsr_gb300 import _lib
+    from pydfcsr_gb300.runtime import ptr, stream_handle
     sets = []
-    cur = run.beam.particle.clone()
+    cur = run.beam.particle
     for k in range(1, steps + 1):
-        R = torch.as_tensor(run.plan.matrix(k), device=cur.device)
-        cur = (R @ cur).contiguous()
+        cur = cur.clone()
+        R = np.ascontiguousarray(run.plan.matrix(k))
+        _lib.call("dfcsr_transport6", R.ctypes.data_as(ctypes.c_void_p), ptr(cur), cur.shape[1],
+                  cur.stride(0), stream_handle())
         sets.append(cur)
     return sets
 
