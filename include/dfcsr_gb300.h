@@ -205,7 +205,9 @@ int dfcsr_interp1d(const double *q, int64_t m, const double *table, int n,
  */
 typedef struct {
     const double *ring64;       /* [cap][nx][nz][5] or NULL                   */
-    const float *ring32;        /* [cap][nx][nz][8] or NULL (see regrid)      */
+    const float *ring32;        /* [cap][nx][nz][8] or NULL (see regrid);     */
+                                /* 32-byte aligned (else the mixed wake       */
+                                /* returns NaN for the job's points)          */
     int cap, head, nt, nx, nz;  /* ring capacity, oldest slot, slices, grid   */
     int pad0;
     double t_min, x_min, z_min; /* build_interpolant (deposit.py:416-421)     */

@@ -2,8 +2,8 @@
 //
 // histogram_cic_2d (pyDFCSR_2D/deposit.py:43-87) scatters four corner weights
 // per particle serially.  Here particles are sorted by their lower cell with
-// a stable LSD radix sort (8-bit digits, per-warp match_any ranking, no
-// atomics), fixed-size chunks of the sorted particles are reduced per lower
+// a stable LSD radix sort (9-bit digits, per-warp match_any ranking, no
+// float atomics), fixed-size chunks of the sorted particles are reduced per lower
 // cell into four moments per weight channel (sum w, w f1, w f2, w f1 f2 of
 // the fractional offsets), and a gather pass forms the four corner sums that
 // land on each output cell.  Same result for the same input on every run; no
@@ -153,21 +153,24 @@ constexpr int RS_THREADS = 256;
 constexpr int RS_ITEMS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_BINS = 256;
+constexpr int RS_BITS = 9;                 // digit width: keys of grids up to 361^2 in 2 passes
+constexpr int RS_BINS = 1 << RS_BITS;
+constexpr uint32_t RS_MASK = RS_BINS - 1;
 
 __global__ void __launch_bounds__(RS_THREADS)
 radix_upsweep(const uint32_t *__restrict__ keys, int64_t n, int shift, int ntiles,
               uint32_t *__restrict__ hist) {
     __shared__ uint32_t cnt[RS_BINS];
-    cnt[threadIdx.x] = 0;
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) cnt[d] = 0;
     __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * RS_TILE;
     for (int r = 0; r < RS_ITEMS; ++r) {
         const int64_t idx = base + (int64_t)r * RS_THREADS + threadIdx.x;
-        if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & 255u], 1u);   // integer: exact
+        if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & RS_MASK], 1u);   // integer: exact
     }
     __syncthreads();
-    hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = cnt[threadIdx.x];
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS)
+        hist[(size_t)d * ntiles + blockIdx.x] = cnt[d];
 }
 
 // One block per digit: exclusive scan of hist[digit][0..ntiles) in place,
@@ -219,16 +222,17 @@ radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ va
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int d = threadIdx.x; d < RS_WARPS * RS_BINS; d += RS_THREADS) (&wcnt[0][0])[d] = 0;
     if (warp == 0) {
-        // exclusive scan of the 256 digit totals (8 per lane)
-        uint32_t loc[8], s = 0;
-        for (int k = 0; k < 8; ++k) { loc[k] = dtot[lane * 8 + k]; s += loc[k]; }
+        // exclusive scan of the digit totals (RS_BINS / 32 per lane)
+        constexpr int PER = RS_BINS / 32;
+        uint32_t loc[PER], s = 0;
+        for (int k = 0; k < PER; ++k) { loc[k] = dtot[lane * PER + k]; s += loc[k]; }
         uint32_t inc = s;
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
             if (lane >= o) inc += t;
         }
         uint32_t run = inc - s;
-        for (int k = 0; k < 8; ++k) { dbase[lane * 8 + k] = run; run += loc[k]; }
+        for (int k = 0; k < PER; ++k) { dbase[lane * PER + k] = run; run += loc[k]; }
     }
     __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)warp * (32 * RS_ITEMS);
@@ -240,7 +244,7 @@ radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ va
         const int64_t idx = base + r * 32 + lane;
         const bool valid = idx < n;
         const uint32_t key = valid ? keys[idx] : 0u;
-        const int d = valid ? (int)((key >> shift) & 255u) : RS_BINS;
+        const int d = valid ? (int)((key >> shift) & RS_MASK) : RS_BINS;
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const int leader = __ffs(peers) - 1;
         uint32_t before = 0;
@@ -254,8 +258,7 @@ radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ va
         v[r] = valid ? vals[idx] : 0u;
     }
     __syncthreads();
-    {
-        const int d = threadIdx.x;   // RS_THREADS == RS_BINS
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) {
         uint32_t run = 0;
         for (int w = 0; w < RS_WARPS; ++w) {
             const uint32_t t = wcnt[w][d];
@@ -466,7 +469,7 @@ static DepositLayout deposit_layout(int64_t n, int nb1, int nb2) {
     int bits = 1;
     while ((1ull << bits) <= (unsigned long long)L.nkeys) ++bits;   // sentinel included
     L.bits = bits;
-    L.passes = (bits + 7) / 8;
+    L.passes = (bits + RS_BITS - 1) / RS_BITS;
     L.ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
     if (L.ntiles < 1) L.ntiles = 1;
     return L;
@@ -568,7 +571,7 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
                                                               start2, inv2, L.nkeys, ka, va);
         uint32_t *kin = ka, *vin = va, *kout = kb, *vout = vb;
         for (int p = 0; p < L.passes; ++p) {
-            const int shift = 8 * p;
+            const int shift = RS_BITS * p;
             radix_upsweep<<<L.ntiles, RS_THREADS, 0, s>>>(kin, n, shift, L.ntiles, hist);
             radix_scan_rows<<<RS_BINS, 1024, 0, s>>>(hist, L.ntiles, dtot);
             radix_scatter<<<L.ntiles, RS_THREADS, 0, s>>>(kin, vin, n, shift, L.ntiles, hist, dtot,

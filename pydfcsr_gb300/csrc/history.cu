@@ -122,8 +122,8 @@ extern "C" int dfcsr_history_regrid(const double *density, const double *density
     DFCSR_CHECK_ARG(snx >= 2 && snz >= 2, "dfcsr_history_regrid: source grid %d x %d too small", snx, snz);
     DFCSR_CHECK_ARG(nxi >= 1 && nzi >= 1, "dfcsr_history_regrid: empty target grid");
     DFCSR_CHECK_ARG(ring64_slot || ring32_slot, "dfcsr_history_regrid: no output ring");
-    DFCSR_CHECK_ARG(!ring32_slot || ((uintptr_t)ring32_slot % 16) == 0,
-                    "dfcsr_history_regrid: ring32 slot must be 16-byte aligned");
+    DFCSR_CHECK_ARG(!ring32_slot || ((uintptr_t)ring32_slot % 32) == 0,
+                    "dfcsr_history_regrid: ring32 slot must be 32-byte aligned");
     const int64_t cells = (int64_t)nxi * nzi;
     ScopedTiming tm("history_regrid", as_stream(stream));
     regrid5<<<(unsigned)((cells + 255) / 256), 256, 0, as_stream(stream)>>>(

@@ -139,6 +139,9 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         gs.nreg = wake_regions(J, s, x, gs.reg);
         bool ok;
         layout(gs.reg, gs.nreg, gs.rm, ok, rec_words);
+        // the integral reads 32-byte cells with one 256-bit load: a ring that
+        // is not 32-byte aligned makes the point invalid (NaN result)
+        if (((uintptr_t)J.ring32 & 31u) != 0) ok = false;
         gs.ok = ok ? 1 : 0;
         PointMeta m;
         m.nreg = gs.nreg;
@@ -279,6 +282,15 @@ struct Fields5 {
     float den, dx, dz, vx, vxx;
 };
 
+// A 32-byte history cell (den, dx_hi, dz, vx | vxx, dx_lo, pad, pad) in one
+// 256-bit non-coherent load; the two pad words are not kept.
+__device__ __forceinline__ void ld_cell(const float4 *p, float4 &a, float2 &b) {
+    float p0, p1;
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(p0), "=f"(p1)
+        : "l"(p));
+}
+
 // a + w (b - a) with one rounding for the product-add.
 __device__ __forceinline__ float lerp1(float a, float b, float w) { return fmaf(w, b - a, a); }
 
@@ -290,24 +302,17 @@ template <bool FF>
 __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint32_t c00, uint32_t c01,
                                            uint32_t c10, uint32_t c11, uint32_t dzc, float td, float xd,
                                            float zd) {
-    // second half of a cell: (vx_x, density_x low part) as one 8-byte load
-    auto hi2 = [&](uint32_t c) { return __ldg(reinterpret_cast<const float2 *>(ring + c + 1)); };
-    const float4 A0 = __ldg(ring + c00);
-    const float2 a0 = hi2(c00);
-    const float4 A1 = __ldg(ring + c00 + dzc);
-    const float2 a1 = hi2(c00 + dzc);
-    const float4 B0 = __ldg(ring + c01);
-    const float2 b0 = hi2(c01);
-    const float4 B1 = __ldg(ring + c01 + dzc);
-    const float2 b1 = hi2(c01 + dzc);
-    const float4 C0 = __ldg(ring + c10);
-    const float2 c0 = hi2(c10);
-    const float4 C1 = __ldg(ring + c10 + dzc);
-    const float2 c1 = hi2(c10 + dzc);
-    const float4 D0 = __ldg(ring + c11);
-    const float2 d0 = hi2(c11);
-    const float4 D1 = __ldg(ring + c11 + dzc);
-    const float2 d1 = hi2(c11 + dzc);
+    // one 32-byte load per cell (the cells are 32-byte aligned)
+    float4 A0, A1, B0, B1, C0, C1, D0, D1;
+    float2 a0, a1, b0, b1, c0, c1, d0, d1;
+    ld_cell(ring + c00, A0, a0);
+    ld_cell(ring + c00 + dzc, A1, a1);
+    ld_cell(ring + c01, B0, b0);
+    ld_cell(ring + c01 + dzc, B1, b1);
+    ld_cell(ring + c10, C0, c0);
+    ld_cell(ring + c10 + dzc, C1, c1);
+    ld_cell(ring + c11, D0, d0);
+    ld_cell(ring + c11 + dzc, D1, d1);
     auto tri = [&](float v00a, float v00b, float v01a, float v01b, float v10a, float v10b,
                    float v11a, float v11b) -> float {
         const float c00_ = lerp1(v00a, v00b, td);
