@@ -156,6 +156,14 @@ class HistoryRing:
         self.head = 0
         self.count = 0
 
+    def slice(self, k, field):
+        """Host copy of one field of logical slice k (0 = oldest)."""
+        f = FIELDS.index(field)
+        slot = (self.head + k) % self.cap
+        if self.ring64 is not None:
+            return self.ring64[slot][..., f].cpu().numpy()
+        return self.ring32[slot][..., f].double().cpu().numpy()
+
     def stacked(self, field):
         """Host copy [count, nx, nz] of one field in time order (compatibility)."""
         f = FIELDS.index(field)
