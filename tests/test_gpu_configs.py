@@ -100,7 +100,11 @@ def _mixed_vs_fp64(name, steps, check_at, near_band=0.0):
 
 @cuda
 def test_double_horn_full_size_mixed_vs_fp64():
-    for k, slope, res in _mixed_vs_fp64("chicane_c3", 24, (12, 24)):
+    """Inside the first bend's drift (3-region branch) and later, once the
+    x-z slope exceeds 1 (4-region chirped branch)."""
+    out = _mixed_vs_fp64("chicane_c3", 40, (12, 40))
+    assert out[0][1] < 1.0 < out[-1][1]
+    for k, slope, res in out:
         e = res[0.0]
         assert e["max_rel"] <= 1e-4 and e["rms_rel"] <= 1e-4, (k, slope, e)
 
@@ -109,8 +113,9 @@ def test_double_horn_full_size_mixed_vs_fp64():
 def test_large_beam_full_size_mixed_vs_fp64_with_band():
     from pydfcsr_gb300.synthetic import workload
     sz = 30e-6
-    out = _mixed_vs_fp64("chicane_c5", 10, (10,), near_band=20 * sz)
+    out = _mixed_vs_fp64("chicane_c5", 120, (10, 120), near_band=20 * sz)
     assert workload("chicane_c5").n_particles == 10_000_000
+    assert out[0][1] < 1.0 < out[-1][1]
     for k, slope, res in out:
         for band, e in res.items():
             assert e["max_rel"] <= 1e-4 and e["rms_rel"] <= 1e-4, (k, band, e)
