@@ -34,6 +34,7 @@ constexpr int MX_CHUNK = 128;       // s' columns staged in shared memory at onc
 constexpr int MX_MAX_ROWS = 1024;   // x' rows per region (2 * xbins)
 constexpr int MX_MAX_COLS = 4096;   // s' columns per region (zbins)
 constexpr int GEO_THREADS = 256;
+constexpr int GEO_MAXB = 6;
 
 // Column record: 28 words (7 float4; stride 112 B keeps 8-lane phases of
 // 16-byte shared loads conflict free).  Row record: 8 words (2 float4).
@@ -63,7 +64,13 @@ __host__ __device__ inline size_t point_record_words(int xbins, int zbins) {
     return (size_t)WAKE_MAX_REGIONS * zbins * CW + (size_t)5 * xbins * RW;
 }
 
-__device__ __forceinline__ int clamp_int(double v) { return (int)fmax(fmin(v, 2.0e9), -2.0e9); }
+// Integer cell of a history coordinate u from its floor fl: clamped to
+// +-2e9 with integer operations; NaN -> 2e9 (outside every grid).
+__device__ __forceinline__ int cell_index(double u, double fl) {
+    const int c = __double2int_rz(fl);   // fl is integral; saturates for huge |u|
+    const bool nan = (__double_as_longlong(u) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+    return nan ? 2000000000 : max(min(c, 2000000000), -2000000000);
+}
 
 // s' of column j and x' of row i: start + k * step (the reference's
 // linspace up to rounding, which the mixed path does not need to reproduce).
@@ -109,6 +116,11 @@ struct GeoShared {
     double xref[WAKE_MAX_REGIONS];
     int col_begin[WAKE_MAX_REGIONS + 1], row_begin[WAKE_MAX_REGIONS + 1];
     int lo[WAKE_MAX_REGIONS], hi[WAKE_MAX_REGIONS];
+    // curvature per column: element index at the region's first column and
+    // the columns where s' crosses the next element ends (GEO_MAXB at most;
+    // more -> per-column lookup)
+    int e_first[WAKE_MAX_REGIONS], nthr[WAKE_MAX_REGIONS];
+    int thr_j[WAKE_MAX_REGIONS][GEO_MAXB];
     double lat_s[6];
     double vx_obs;
     int nreg, ok;
@@ -157,6 +169,28 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
             gs.xref[r] = gs.ax_x[r].at(R.nxp / 2);
             gs.col_begin[r] = cb;
             gs.row_begin[r] = rb;
+            // rho_at over the region's columns s'(j) = start + j step (non-
+            // decreasing in j): element index = number of element ends <= s'
+            {
+                const Axis &A = gs.ax_s[r];
+                const double s_first = A.at(0), s_last = A.at(R.nsp - 1);
+                int ef = 0, nb = (A.step > 0.0) ? 0 : -1;   // descending / flat: per column
+                for (int e = 0; e < J.nelement && nb >= 0; ++e) {
+                    const double d = J.distance[e];
+                    if (d <= s_first) ++ef;
+                    else if (d <= s_last) {
+                        if (nb == GEO_MAXB) { nb = -1; break; }
+                        // first column j with s'(j) >= d
+                        int jj = (int)ceil((d - A.start) / A.step);
+                        jj = max(0, min(jj, R.nsp - 1));
+                        while (jj > 0 && A.at(jj - 1) >= d) --jj;
+                        while (jj < R.nsp - 1 && A.at(jj) < d) ++jj;
+                        gs.thr_j[r][nb++] = jj;
+                    }
+                }
+                gs.e_first[r] = ef;
+                gs.nthr[r] = nb;
+            }
             gs.lo[r] = R.nxp;
             gs.hi[r] = -1;
             cb += R.nsp;
@@ -217,6 +251,14 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         const double ut0 = (T0 - r0) * inv_t;
         const double uz0 = ((spj - Tz) + r0) * inv_z;
         const double tfl = floor(ut0), zfl = floor(uz0);
+        float rho_f;
+        if (gs.nthr[r] >= 0) {
+            int e = gs.e_first[r];
+            for (int q = 0; q < gs.nthr[r]; ++q) e += (j >= gs.thr_j[r][q]) ? 1 : 0;
+            rho_f = (e < J.nelement) ? (float)J.rho[e] : 0.f;
+        } else {
+            rho_f = (float)rho_at(J, spj);
+        }
         const double a = vxo * tpx + vyo * tpy, bb = vxo * npx + vyo * npy;
         const double e = tpx * npx + tpy * npy, g = npx * npx + npy * npy;
         const double h = tpx * tpx + tpy * tpy;
@@ -225,10 +267,9 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         const double q2 = nsx * tpx + nsy * tpy;
         const bool near = J.near_band > 0.0 && fabs(spj - s) < J.near_band;
         float4 *o = reinterpret_cast<float4 *>(prec + gs.rm[r].col_off) + (size_t)j * (CW / 4);
-        o[0] = make_float4(__int_as_float(clamp_int(tfl)), __int_as_float(clamp_int(zfl)),
+        o[0] = make_float4(__int_as_float(cell_index(ut0, tfl)), __int_as_float(cell_index(uz0, zfl)),
                            (float)(ut0 - tfl), (float)(uz0 - zfl));
-        o[1] = make_float4((float)r0, (float)(rx0 * npx + ry0 * npy), (float)(g - 1.0),
-                           (float)rho_at(J, spj));
+        o[1] = make_float4((float)r0, (float)(rx0 * npx + ry0 * npy), (float)(g - 1.0), rho_f);
         o[2] = make_float4((float)a, (float)bb, (float)e, (float)g);
         o[3] = make_float4((float)h, (float)(bb - a * e), (float)((a * g - 1.0) + bb * e),
                            (float)(bb * g));
@@ -289,6 +330,8 @@ __device__ __forceinline__ void ld_cell(const float4 *p, float4 &a, float2 &b) {
     asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
         : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(p0), "=f"(p1)
         : "l"(p));
+    (void)p0;
+    (void)p1;
 }
 
 // a + w (b - a) with one rounding for the product-add.
