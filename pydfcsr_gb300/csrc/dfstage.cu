@@ -129,22 +129,27 @@ sg_axis(FieldSet fs, int nx, int nz, int w, const double *__restrict__ coef,
         else { c = idx / SG_TILE; rl = idx % SG_TILE; }
         const int l = l0 + rl;
         if (l >= L || c >= ncol) continue;
-        double acc;
+        // the window's weights (interior, left edge or right edge map) and
+        // its first sample; two fused multiply-add chains (even / odd taps)
+        const double *x, *e;
         if (l >= m && l < L - m) {
-            const double *x = tile + (l - m - lo) * ld + c;
-            acc = __dmul_rn(x[0], coef[0]);
-            for (int k = 1; k < w; ++k) acc = __dadd_rn(acc, __dmul_rn(x[k * ld], coef[k]));
+            x = tile + (l - m - lo) * ld + c;
+            e = coef;
         } else if (l < m) {
-            const double *x = tile + (0 - lo) * ld + c;
-            const double *e = elo + (size_t)l * w;
-            acc = __dmul_rn(x[0], e[0]);
-            for (int k = 1; k < w; ++k) acc = __dadd_rn(acc, __dmul_rn(x[k * ld], e[k]));
+            x = tile + (0 - lo) * ld + c;
+            e = elo + (size_t)l * w;
         } else {
-            const double *x = tile + (L - w - lo) * ld + c;
-            const double *e = ehi + (size_t)(l - (L - m)) * w;
-            acc = __dmul_rn(x[0], e[0]);
-            for (int k = 1; k < w; ++k) acc = __dadd_rn(acc, __dmul_rn(x[k * ld], e[k]));
+            x = tile + (L - w - lo) * ld + c;
+            e = ehi + (size_t)(l - (L - m)) * w;
         }
+        double a0 = __dmul_rn(x[0], e[0]), a1 = 0.0;
+        int k = 1;
+        for (; k + 1 < w; k += 2) {
+            a1 = __fma_rn(x[k * ld], e[k], a1);
+            a0 = __fma_rn(x[(k + 1) * ld], e[k + 1], a0);
+        }
+        if (k < w) a1 = __fma_rn(x[k * ld], e[k], a1);
+        const double acc = __dadd_rn(a0, a1);
         g[(size_t)l * sL + (size_t)(c0 + c) * sM] = acc;
     }
 }

@@ -326,12 +326,11 @@ struct Fields5 {
 // A 32-byte history cell (den, dx_hi, dz, vx | vxx, dx_lo, pad, pad) in one
 // 256-bit non-coherent load; the two pad words are not kept.
 __device__ __forceinline__ void ld_cell(const float4 *p, float4 &a, float2 &b) {
-    float p0, p1;
+    float4 t;
     asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(p0), "=f"(p1)
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
         : "l"(p));
-    (void)p0;
-    (void)p1;
+    b = make_float2(t.x, t.y);
 }
 
 // a + w (b - a) with one rounding for the product-add.
