@@ -483,6 +483,13 @@ def serving_leg(n_requests, rate_hz, fp64_sample, seed=4):
     out = {"stream": f"{n_requests} requests, Poisson arrivals at {rate_hz:g}/s (seed {seed}), "
                      "8 DF steps + 7 wakes each, 100x100 integration bins",
            "mixed": full}
+    # capacity: the same requests all waiting at t = 0 (closed loop)
+    burst = [RequestSpec.from_dict({**r, "arrival_s": 0.0}) for r in reqs]
+    srv = WakeServer(burst, precision="mixed")
+    out["capacity"] = srv.run()
+    out["capacity"]["definition"] = "the same requests all arriving at t = 0"
+    del srv
+    torch.cuda.empty_cache()
     if fp64_sample > 0:
         sample = [RequestSpec.from_dict({**r, "arrival_s": 0.0}) for r in reqs[:fp64_sample]]
         m = WakeServer(sample, precision="mixed")

@@ -177,6 +177,7 @@ class CSR2D:
         if formation_length is not None:
             self.formation_length = formation_length
         b = self.beam
+        b.sync_status()
         t = self.DF_tracker
         # the beam's moments are of these same (x, z) tensors
         t.get_DF(x=b.x, z=b.z, px=b.px, t=b.position, moments=b._moments)

@@ -52,17 +52,33 @@ class Beam:
             self.particle = self.particle.clone()
             self._owned = True
 
-    def update_status(self, stream=None):
+    def update_status(self, stream=None, wait=True):
         """Beam statistics from one device moments call; waits for it (and
-        for whatever precedes it on ``stream``, default the current one)."""
-        if stream is not None:
-            with torch.cuda.stream(stream):
-                m = beam_moments(self.particle[0], self.particle[4], ws=self.ws)
-                st = m.cpu().numpy()
-        else:
+        for whatever precedes it on ``stream``, default the current one).
+
+        ``wait=False`` only enqueues the moments and their copy to pinned host
+        memory; :meth:`sync_status` (or the next update) completes them."""
+        s = stream if stream is not None else torch.cuda.current_stream()
+        with torch.cuda.stream(s):
             m = beam_moments(self.particle[0], self.particle[4], ws=self.ws)
-            st = m.cpu().numpy()
+            host = torch.empty(m.numel(), dtype=torch.float64, pin_memory=True)
+            host.copy_(m, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(s)
         self._moments_dev = m
+        self._pending_status = (host, ev)
+        if wait:
+            self.sync_status()
+
+    def sync_status(self):
+        """Wait for the moments enqueued by ``update_status(wait=False)`` and
+        set the statistics from them."""
+        if getattr(self, "_pending_status", None) is None:
+            return
+        host, ev = self._pending_status
+        ev.synchronize()
+        self._pending_status = None
+        st = host.numpy().copy()
         self._moments = st
         self._mean_x, self._mean_z = float(st[1]), float(st[2])
         self._sigma_x, self._sigma_z = float(st[3]), float(st[4])
@@ -116,11 +132,17 @@ class Beam:
     py = property(lambda self: self.particle[3])
     z = property(lambda self: self.particle[4])
     pz = property(lambda self: self.particle[5])
-    mean_x = property(lambda self: self._mean_x)
-    mean_z = property(lambda self: self._mean_z)
-    sigma_x = property(lambda self: self._sigma_x)
-    sigma_z = property(lambda self: self._sigma_z)
-    slope = property(lambda self: self._slope.copy())
+    def _stat(name):
+        def get(self):
+            self.sync_status()
+            return getattr(self, name)
+        return property(get)
+
+    mean_x = _stat("_mean_x")
+    mean_z = _stat("_mean_z")
+    sigma_x = _stat("_sigma_x")
+    sigma_z = _stat("_sigma_z")
+    slope = property(lambda self: (self.sync_status(), self._slope.copy())[1])
     charge = property(lambda self: self._charge)
     init_energy = property(lambda self: self._init_energy)
 
@@ -131,8 +153,10 @@ class Beam:
 
     @property
     def sigma_x_transform(self):
+        self.sync_status()
         return float(self._moments[10])
 
     @property
     def mean_x_transform(self):
+        self.sync_status()
         return float(self._moments[9])

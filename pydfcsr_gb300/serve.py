@@ -190,17 +190,26 @@ class _Live:
         self.finished_at = None
         self.done_event = None
 
-    def advance(self):
-        """Transport to the next step, then deposit + DF + history update, on
-        this request's stream (the host waits only for the beam moments)."""
+    def advance_launch(self):
+        """Transport to the next step and enqueue its beam moments on this
+        request's stream (no host wait)."""
         import torch
         with torch.cuda.stream(self.stream):
             k = self.k + 1
-            self.beam.track(self.plan.matrix(k), 0.0, update_step=True)
+            self.beam.transport(self.plan.matrix(k))
+            self.beam.update_status(wait=False)
             self.beam.position = float(self.plan.positions[k])
-            self.csr.update_history(self.plan.formation_length(k, self.beam.sigma_z))
-            self.csr.get_CSR_mesh()
+            self.beam.step = k
             self.k = k
+
+    def advance_finish(self):
+        """Deposit + DF + history update of the step launched by
+        advance_launch (the host waits for this request's moments only)."""
+        import torch
+        with torch.cuda.stream(self.stream):
+            self.beam.sync_status()
+            self.csr.update_history(self.plan.formation_length(self.k, self.beam.sigma_z))
+            self.csr.get_CSR_mesh()
             self.done_event = torch.cuda.Event()
             self.done_event.record(self.stream)
 
@@ -270,33 +279,46 @@ class _BatchedWake:
             _lib.call("dfcsr_wake_fp64", ptr(self.jobs), ptr(self.jop), ptr(self.s), ptr(self.x), n,
                       ptr(self.dE), ptr(self.xk), h)
 
-    def run(self, jobs_raw, s, x, jop, stream):
-        """Upload one tick's jobs and points, run the wake, return host
-        (dE, x_kick) for the n real points."""
+    def run(self, jobs_raw, meshes, stream):
+        """One tick: the job structs and job index per point go up from
+        pinned memory, every request's mesh is built on the device straight
+        into the static point buffers (``meshes``: one ``CSR2D._mesh``
+        parameter tuple per job), the padding repeats the first point, the
+        wake runs (graph replay) and (dE, x_kick) of the real points come
+        back.  Returns host arrays."""
+        import ctypes
         import torch
-        n = s.size
+        from . import _lib
+        from .runtime import ptr
+        sizes = [m[2] * m[5] for m in meshes]
+        n = int(sum(sizes))
         if n > self.cap or len(jobs_raw) > self.max_jobs * self.job_bytes:
             raise RuntimeError("tick exceeds the static wake buffers")
         padded = int(math.ceil(n / self.chunk) * self.chunk)
-        # stage s | x | jop | jobs in one pinned block, then four copies
         hb = self.host.numpy()
-        o = 0
-        for arr, width in ((s, 8), (x, 8)):
-            v = hb[o:o + padded * width].view(np.float64)
-            v[:n] = arr
-            v[n:] = arr[0]
-            o += padded * width
-        vj = hb[o:o + padded * 4].view(np.int32)
-        vj[:n] = jop
-        vj[n:] = jop[0]
-        o += padded * 4
+        vj = hb[:padded * 4].view(np.int32)
+        off = 0
+        for ji, m in enumerate(sizes):
+            vj[off:off + m] = ji
+            off += m
+        vj[n:] = 0
+        o = padded * 4
         hb[o:o + len(jobs_raw)] = np.frombuffer(jobs_raw, dtype=np.uint8)
+        h = ctypes.c_void_p(stream.cuda_stream)
         with torch.cuda.stream(stream):
             ht = self.host
-            self.s[:padded].copy_(ht[:padded * 8].view(torch.float64), non_blocking=True)
-            self.x[:padded].copy_(ht[padded * 8:padded * 16].view(torch.float64), non_blocking=True)
-            self.jop[:padded].copy_(ht[padded * 16:padded * 20].view(torch.int32), non_blocking=True)
+            self.jop[:padded].copy_(ht[:padded * 4].view(torch.int32), non_blocking=True)
             self.jobs[:len(jobs_raw)].copy_(ht[o:o + len(jobs_raw)], non_blocking=True)
+            off = 0
+            for m, size in zip(meshes, sizes):
+                x0, x1, xb, z0, z1, zb, p0, p1, pos = m
+                _lib.call("dfcsr_csr_mesh", x0, x1, xb, z0, z1, zb, p0, p1, pos,
+                          ctypes.c_void_p(self.s.data_ptr() + 8 * off),
+                          ctypes.c_void_p(self.x.data_ptr() + 8 * off), h)
+                off += size
+            if padded > n:
+                self.s[n:padded].copy_(self.s[:1].expand(padded - n))
+                self.x[n:padded].copy_(self.x[:1].expand(padded - n))
             k = padded // self.chunk
             if not self.use_graphs or not self.warm:
                 # the first call runs eagerly: one-time library set-up happens
@@ -362,29 +384,25 @@ class WakeServer:
         from .CSR import wake_job
         if not reqs:
             return
-        jobs, S, Xs, J = [], [], [], []
-        for ji, lv in enumerate(reqs):
+        jobs, meshes = [], []
+        for lv in reqs:
             c = lv.csr
             b = c.beam
             ip = c.integration_params
             jobs.append(wake_job(c.DF_tracker, c.lattice, b.position, b._sigma_z, b._sigma_x,
                                  b._slope[0], b._mean_x, c.formation_length, ip.n_formation_length,
                                  c.CSR_scaling, ip.zbins, ip.xbins))
-            S.append(b.position + c.CSR_zmesh)
-            Xs.append(c.CSR_xmesh)
-            J.append(np.full(c.CSR_zmesh.size, ji, dtype=np.int32))
-        import torch
+            meshes.append(c._mesh)
         for lv in reqs:
             self.stream.wait_event(lv.done_event)
         t = time.perf_counter()
-        dE, xk = self.wake.run(b"".join(bytes(j) for j in jobs), np.concatenate(S),
-                               np.concatenate(Xs), np.concatenate(J), self.stream)
+        dE, xk = self.wake.run(b"".join(bytes(j) for j in jobs), meshes, self.stream)
         self.wake_s += time.perf_counter() - t
         self.launch_points.append(dE.size)
         off = 0
         for lv in reqs:
-            m = lv.csr.CSR_zmesh.size
             shape = (lv.csr.CSR_params.xbins, lv.csr.CSR_params.zbins)
+            m = shape[0] * shape[1]
             lv.results.append((lv.k, dE[off:off + m].reshape(shape), xk[off:off + m].reshape(shape)))
             lv.points += m
             off += m
@@ -403,8 +421,13 @@ class WakeServer:
                     time.sleep(max(0.0, nxt - self._clock()))
                 continue
             lives = [self.live[s.id] for s in sched.active]
+            # every request's transport + moments first, then each request's
+            # DF step: the moments of all beams run while the host waits for
+            # the first one
             for lv in lives:
-                lv.advance()
+                lv.advance_launch()
+            for lv in lives:
+                lv.advance_finish()
             self._wake_tick([lv for lv in lives if lv.wants_wake()])
             self.ticks += 1
             for lv in lives:
