@@ -155,14 +155,18 @@ int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, double *vx,
  *
  * The source fields are five device arrays [snx][snz]; the target is one
  * slot of the device history ring.  The per-axis interval indices and
- * normalised distances (tensor-product grids) are precomputed by the host:
- * ix[nxi], wx[nxi], oobx[nxi] (1 = outside), iz[nzi], wz[nzi], oobz[nzi].
+ * normalised distances (tensor-product grids) are device tables computed
+ * beforehand (dfcsr_rgi_axis_linspace, or by the host): ix[nxi], wx[nxi],
+ * oobx[nxi] (1 = outside), iz[nzi], wz[nzi], oobz[nzi].
  * vx_x_fill is a DEVICE pointer to the fill value of vx_x (its mean).
  * ring64: [slot][nxi][nzi][5] doubles (or NULL); ring32: [slot][nxi][nzi][8]
  * floats (or NULL): fields 0..4, then in slot 5 the low part of density_x
  * (density_x - (double)(float)density_x), slots 6..7 zero.  Field order:
- * density, density_x, density_z, vx, vx_x.
- */
+ * density, density_x, density_z, vx, vx_x.  With ring64 the values follow
+ * RegularGridInterpolator's term order exactly; with ring32 only, the
+ * bilinear weights are applied as fused multiply-adds (the FP32 cells are
+ * unchanged to within their rounding). */
+
 /* The axis tables of dfcsr_history_regrid when the source grid and the
  * target grid are numpy linspaces (get_DF's x_grids / z_grids and
  * append_interpolant's x_grid_interp / z_grid_interp, deposit.py:170-171,

@@ -14,6 +14,12 @@
 
 namespace dfcsr {
 
+// EXACT: RegularGridInterpolator's term order with every product rounded
+// (the FP64 ring of the drop-in).  Otherwise (FP32 ring only) the four
+// bilinear weights are formed once and each field is one multiply and three
+// fused multiply-adds in FP64 - well inside the FP32 cell's resolution, and
+// density_x keeps the ~1e-16 relative accuracy its hi + lo pair carries.
+template <bool EXACT>
 __global__ void regrid5(const double *__restrict__ f0, const double *__restrict__ f1,
                         const double *__restrict__ f2, const double *__restrict__ f3,
                         const double *__restrict__ f4, int snz,
@@ -36,15 +42,24 @@ __global__ void regrid5(const double *__restrict__ f0, const double *__restrict_
         const double u0 = 1.0 - y0, u1 = 1.0 - y1;
         const size_t k00 = (size_t)i * snz + j, k01 = k00 + 1, k10 = k00 + snz, k11 = k10 + 1;
         const double *F[5] = {f0, f1, f2, f3, f4};
+        if (EXACT) {
 #pragma unroll
-        for (int q = 0; q < 5; ++q) {
-            const double *p = F[q];
-            double r = 0.0;
-            r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k00], u0), u1));
-            r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k01], u0), y1));
-            r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k10], y0), u1));
-            r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k11], y0), y1));
-            v[q] = r;
+            for (int q = 0; q < 5; ++q) {
+                const double *p = F[q];
+                double r = 0.0;
+                r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k00], u0), u1));
+                r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k01], u0), y1));
+                r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k10], y0), u1));
+                r = __dadd_rn(r, __dmul_rn(__dmul_rn(p[k11], y0), y1));
+                v[q] = r;
+            }
+        } else {
+            const double w00 = u0 * u1, w01 = u0 * y1, w10 = y0 * u1, w11 = y0 * y1;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                const double *p = F[q];
+                v[q] = fma(p[k11], w11, fma(p[k10], w10, fma(p[k01], w01, p[k00] * w00)));
+            }
         }
     }
     if (out64) {
@@ -126,9 +141,15 @@ extern "C" int dfcsr_history_regrid(const double *density, const double *density
                     "dfcsr_history_regrid: ring32 slot must be 32-byte aligned");
     const int64_t cells = (int64_t)nxi * nzi;
     ScopedTiming tm("history_regrid", as_stream(stream));
-    regrid5<<<(unsigned)((cells + 255) / 256), 256, 0, as_stream(stream)>>>(
-        density, density_x, density_z, vx, vx_x, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,
-        vx_x_fill, ring64_slot, ring32_slot);
+    const unsigned blocks = (unsigned)((cells + 255) / 256);
+    if (ring64_slot)
+        regrid5<true><<<blocks, 256, 0, as_stream(stream)>>>(
+            density, density_x, density_z, vx, vx_x, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,
+            vx_x_fill, ring64_slot, ring32_slot);
+    else
+        regrid5<false><<<blocks, 256, 0, as_stream(stream)>>>(
+            density, density_x, density_z, vx, vx_x, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,
+            vx_x_fill, ring64_slot, ring32_slot);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }

@@ -147,57 +147,63 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         obs_vx[b] = gs.vx_obs;
     } else if (threadIdx.x == 64) {
         lattice_lerp(J, s, gs.lat_s);
-    } else if (threadIdx.x == 0) {
-        gs.nreg = wake_regions(J, s, x, gs.reg);
-        bool ok;
-        layout(gs.reg, gs.nreg, gs.rm, ok, rec_words);
-        // the integral reads 32-byte cells with one 256-bit load: a ring that
-        // is not 32-byte aligned makes the point invalid (NaN result)
-        if (((uintptr_t)J.ring32 & 31u) != 0) ok = false;
-        gs.ok = ok ? 1 : 0;
-        PointMeta m;
-        m.nreg = gs.nreg;
-        m.valid = gs.ok;
-        for (int k = 0; k < WAKE_MAX_REGIONS; ++k)
-            m.reg[k] = (k < gs.nreg) ? gs.rm[k] : RegionMeta{0, 0, 0, 0};
-        meta[b] = m;
-        int cb = 0, rb = 0;
-        for (int r = 0; r < gs.nreg; ++r) {
+    } else if (threadIdx.x < 32) {
+        // warp 0: lane 0 finds the regions and the record layout, then one
+        // lane per region sets up that region's axes and element thresholds
+        if (threadIdx.x == 0) {
+            gs.nreg = wake_regions(J, s, x, gs.reg);
+            bool ok;
+            layout(gs.reg, gs.nreg, gs.rm, ok, rec_words);
+            // the integral reads 32-byte cells with one 256-bit load: a ring
+            // that is not 32-byte aligned makes the point invalid (NaN result)
+            if (((uintptr_t)J.ring32 & 31u) != 0) ok = false;
+            gs.ok = ok ? 1 : 0;
+            PointMeta m;
+            m.nreg = gs.nreg;
+            m.valid = gs.ok;
+            for (int k = 0; k < WAKE_MAX_REGIONS; ++k)
+                m.reg[k] = (k < gs.nreg) ? gs.rm[k] : RegionMeta{0, 0, 0, 0};
+            meta[b] = m;
+            int cb = 0, rb = 0;
+            for (int r = 0; r < gs.nreg; ++r) {
+                gs.col_begin[r] = cb;
+                gs.row_begin[r] = rb;
+                cb += gs.reg[r].nsp;
+                rb += gs.reg[r].nxp;
+            }
+            gs.col_begin[gs.nreg] = cb;
+            gs.row_begin[gs.nreg] = rb;
+        }
+        __syncwarp();
+        const int r = threadIdx.x;
+        if (r < gs.nreg) {
             const Region &R = gs.reg[r];
-            gs.ax_s[r] = make_axis(R.sl, R.sr, R.nsp);
+            const Axis A = make_axis(R.sl, R.sr, R.nsp);
+            gs.ax_s[r] = A;
             gs.ax_x[r] = make_axis(R.xl, R.xr, R.nxp);
             gs.xref[r] = gs.ax_x[r].at(R.nxp / 2);
-            gs.col_begin[r] = cb;
-            gs.row_begin[r] = rb;
-            // rho_at over the region's columns s'(j) = start + j step (non-
-            // decreasing in j): element index = number of element ends <= s'
-            {
-                const Axis &A = gs.ax_s[r];
-                const double s_first = A.at(0), s_last = A.at(R.nsp - 1);
-                int ef = 0, nb = (A.step > 0.0) ? 0 : -1;   // descending / flat: per column
-                for (int e = 0; e < J.nelement && nb >= 0; ++e) {
-                    const double d = J.distance[e];
-                    if (d <= s_first) ++ef;
-                    else if (d <= s_last) {
-                        if (nb == GEO_MAXB) { nb = -1; break; }
-                        // first column j with s'(j) >= d
-                        int jj = (int)ceil((d - A.start) / A.step);
-                        jj = max(0, min(jj, R.nsp - 1));
-                        while (jj > 0 && A.at(jj - 1) >= d) --jj;
-                        while (jj < R.nsp - 1 && A.at(jj) < d) ++jj;
-                        gs.thr_j[r][nb++] = jj;
-                    }
-                }
-                gs.e_first[r] = ef;
-                gs.nthr[r] = nb;
-            }
             gs.lo[r] = R.nxp;
             gs.hi[r] = -1;
-            cb += R.nsp;
-            rb += R.nxp;
+            // rho_at over the region's columns s'(j) = start + j step (non-
+            // decreasing in j): element index = number of element ends <= s'
+            const double s_first = A.at(0), s_last = A.at(R.nsp - 1);
+            int ef = 0, nb = (A.step > 0.0) ? 0 : -1;   // descending / flat: per column
+            for (int e = 0; e < J.nelement && nb >= 0; ++e) {
+                const double d = J.distance[e];
+                if (d <= s_first) ++ef;
+                else if (d <= s_last) {
+                    if (nb == GEO_MAXB) { nb = -1; break; }
+                    // first column j with s'(j) >= d
+                    int jj = (int)ceil((d - A.start) / A.step);
+                    jj = max(0, min(jj, R.nsp - 1));
+                    while (jj > 0 && A.at(jj - 1) >= d) --jj;
+                    while (jj < R.nsp - 1 && A.at(jj) < d) ++jj;
+                    gs.thr_j[r][nb++] = jj;
+                }
+            }
+            gs.e_first[r] = ef;
+            gs.nthr[r] = nb;
         }
-        gs.col_begin[gs.nreg] = cb;
-        gs.row_begin[gs.nreg] = rb;
     }
     __syncthreads();
     if (!gs.ok) return;
