@@ -339,11 +339,12 @@ __device__ __forceinline__ void ld_cell(const float4 *p, float4 &a, float2 &b) {
     b = make_float2(t.x, t.y);
 }
 
+// a + w (b - a) with one rounding for the product-add.
+__device__ __forceinline__ float lerp1(float a, float b, float w) { return fmaf(w, b - a, a); }
+
 // Trilinear FP32 gather of the five fields from ring32 [slot][nx][nz][8]
-// (cell: den, dx_hi, dz, vx | vxx, dx_lo, 0, 0): eight 32-byte cell loads,
-// then each field as the weighted sum of its corners (weights from the t,
-// x and z fractions; the reference's index rule).  In the far region (FF)
-// density_x uses its stored hi + lo pair in offset form.
+// (cell: den, dx_hi, dz, vx | vxx, dx_lo, 0, 0), interpolating t, then x,
+// then z like the reference; density_x in float-float when FF.
 // c<x><t>: float4 index of the z0 cell at x0/x1, t0/t1; dzc: float4 step to z1.
 template <bool FF>
 __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint32_t c00, uint32_t c01,
@@ -360,22 +361,15 @@ __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint
     ld_cell(ring + c10 + dzc, C1, c1);
     ld_cell(ring + c11, D0, d0);
     ld_cell(ring + c11 + dzc, D1, d1);
-    // trilinear weights of the eight corners (t, then x, then z as in the
-    // reference; as weights: one FMA per corner and field)
-    const float ut = 1.f - td, ux = 1.f - xd, uz = 1.f - zd;
-    const float q00 = ux * uz, q01 = ux * zd, q10 = xd * uz, q11 = xd * zd;
-    const float wA0 = ut * q00, wB0 = td * q00, wA1 = ut * q01, wB1 = td * q01;
-    const float wC0 = ut * q10, wD0 = td * q10, wC1 = ut * q11, wD1 = td * q11;
-    auto tri = [&](float vA0, float vB0, float vA1, float vB1, float vC0, float vD0, float vC1,
-                   float vD1) -> float {
-        float r = vA0 * wA0;
-        r = fmaf(vB0, wB0, r);
-        r = fmaf(vA1, wA1, r);
-        r = fmaf(vB1, wB1, r);
-        r = fmaf(vC0, wC0, r);
-        r = fmaf(vD0, wD0, r);
-        r = fmaf(vC1, wC1, r);
-        return fmaf(vD1, wD1, r);
+    auto tri = [&](float v00a, float v00b, float v01a, float v01b, float v10a, float v10b,
+                   float v11a, float v11b) -> float {
+        const float c00_ = lerp1(v00a, v00b, td);
+        const float c01_ = lerp1(v01a, v01b, td);
+        const float c10_ = lerp1(v10a, v10b, td);
+        const float c11_ = lerp1(v11a, v11b, td);
+        const float e0 = lerp1(c00_, c10_, xd);
+        const float e1 = lerp1(c01_, c11_, xd);
+        return lerp1(e0, e1, zd);
     };
     Fields5 r;
     r.den = tri(A0.x, B0.x, A1.x, B1.x, C0.x, D0.x, C1.x, D1.x);
@@ -385,17 +379,17 @@ __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint
     if (FF) {
         // density_x stored as hi + lo: interpolate the offsets from the high
         // part of the first corner, (hi_c - h) + lo_c (the subtraction is
-        // exact for neighbouring values within a factor 2), so only small
-        // numbers are rounded and the result h + D is rounded once - a
-        // correctly rounded FP32 value of the FP64 interpolant
+        // exact for neighbouring values within a factor 2), so the lerp
+        // chain rounds only small numbers and the result h + D is rounded
+        // once - a correctly rounded FP32 value of the FP64 interpolant
         const float h = A0.y;
         r.dx = __fadd_rn(h, tri(a0.y, __fadd_rn(__fsub_rn(B0.y, h), b0.y),
                                 __fadd_rn(__fsub_rn(A1.y, h), a1.y), __fadd_rn(__fsub_rn(B1.y, h), b1.y),
                                 __fadd_rn(__fsub_rn(C0.y, h), c0.y), __fadd_rn(__fsub_rn(D0.y, h), d0.y),
                                 __fadd_rn(__fsub_rn(C1.y, h), c1.y), __fadd_rn(__fsub_rn(D1.y, h), d1.y)));
     } else {
-        // outside the far region the high part alone is ample
-        r.dx = tri(A0.y, B0.y, A1.y, B1.y, C0.y, D0.y, C1.y, D1.y);
+        r.dx = tri(A0.y + a0.y, B0.y + b0.y, A1.y + a1.y, B1.y + b1.y, C0.y + c0.y, D0.y + d0.y,
+                   C1.y + c1.y, D1.y + d1.y);
     }
     return r;
 }
@@ -450,7 +444,6 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const RingV
         if (ws == 0.f) continue;
         const float4 g1 = cr[1], q2 = cr[2], q3 = cr[3], q4 = cr[4];
         const int iend = min(i0 + MX_ROWBLK, i_hi);
-        float pz = 0.f, px = 0.f;   // the unit's few terms, then one compensated add
         for (int i = i0; i < iend; ++i) {
             const float4 *rr = sm.row + i * (RW / 4);
             const float4 ra = rr[0];
@@ -495,11 +488,9 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const RingV
                              F.den * F.vxx;
             const float Ix = scale * inv_r * inv_r * (q1 * inv_r * F.den + pd * M);
             const float w = wx * ws;
-            pz = fmaf(w, Iz, pz);
-            px = fmaf(w, Ix, px);
+            kahan(sz, cz, w * Iz);
+            kahan(sx, cx, w * Ix);
         }
-        kahan(sz, cz, pz);
-        kahan(sx, cx, px);
     }
 }
 
