@@ -304,6 +304,11 @@ __global__ void cell_ranges(const uint32_t *__restrict__ keys, int64_t n,
 constexpr int SEG_K = 16;
 constexpr int SEG_THREADS = 256;
 constexpr int SEG_TILE = SEG_K * SEG_THREADS;
+// the chunk parts (8 doubles per SEG_K particles) live in the idle pair of
+// 4-byte sort buffers after the sort: each buffer must hold a chunk's part
+static_assert(SEG_K * 4 >= 8 * 8, "chunk parts do not fit the idle sort buffers");
+// the staged keys and values of a tile must fit the static shared memory
+static_assert(2 * (SEG_TILE + SEG_TILE / SEG_K) * 4 <= 48 * 1024, "seg_sums tile too large");
 
 // Per-cell moments of the fractional offsets f = c - floor(c) for each
 // weight channel: [sum w, sum w f1, sum w f2, sum w f1 f2].  The CIC corner
