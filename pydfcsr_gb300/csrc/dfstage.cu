@@ -33,12 +33,19 @@ __device__ __forceinline__ double block_max(double v, double *red) {
 }
 
 // OP 0: max(f); OP 1: sum(g) over f > thr2 and count (thr2 = sc[6] / vth * 8);
-// OP 2: sum(f).  part[b * 2 + {0, 1}].
+// OP 2: sum(f).  Final values: OP 0 -> sc[slot] = max; OP 1 -> sc[2] = thr2,
+// sc[3] = sum / count (NaN when empty, like numpy.mean of an empty
+// selection); OP 2 -> sc[slot] = sum / n.
+// Single-launch form: every block writes its partial, the last block to
+// finish (completion counter, reset by that block) adds the partials in
+// block order - the same result as reduce_partial + reduce_final.
 template <int OP>
 __global__ void __launch_bounds__(256)
-reduce_partial(const double *__restrict__ f, const double *__restrict__ g, int n,
-               const double *__restrict__ sc, double vth, double *__restrict__ part) {
+reduce_once(const double *__restrict__ f, const double *__restrict__ g, int n,
+            double *__restrict__ sc, double vth, double *__restrict__ part, int slot,
+            unsigned int *__restrict__ counter) {
     __shared__ double red[8];
+    __shared__ bool last;
     double a = (OP == 0) ? -INFINITY : 0.0, c = 0.0;
     double thr2 = 0.0;
     if (OP == 1) thr2 = __dmul_rn(__ddiv_rn(sc[6], vth), 8.0);
@@ -56,24 +63,21 @@ reduce_partial(const double *__restrict__ f, const double *__restrict__ g, int n
     if (threadIdx.x == 0) {
         part[blockIdx.x * 2 + 0] = a;
         part[blockIdx.x * 2 + 1] = c;
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
     }
-}
-
-// Final pass (one warp): OP 0 -> sc[slot] = max; OP 1 -> sc[2] = thr2,
-// sc[3] = sum / count (NaN when empty, like numpy.mean of an empty
-// selection); OP 2 -> sc[slot] = sum / n.
-template <int OP>
-__global__ void reduce_final(const double *__restrict__ part, int nparts, int n, double *__restrict__ sc,
-                             int slot, double vth) {
-    if (threadIdx.x != 0) return;
-    double a = part[0], c = part[1];
-    for (int k = 1; k < nparts; ++k) {
-        if (OP == 0) a = fmax(a, part[2 * k]);
-        else { a += part[2 * k]; c += part[2 * k + 1]; }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double A = __ldcg(part), C = __ldcg(part + 1);
+    for (int k = 1; k < (int)gridDim.x; ++k) {
+        if (OP == 0) A = fmax(A, __ldcg(part + 2 * k));
+        else { A += __ldcg(part + 2 * k); C += __ldcg(part + 2 * k + 1); }
     }
-    if (OP == 0) sc[slot] = a;
-    else if (OP == 1) { sc[2] = __dmul_rn(__ddiv_rn(sc[6], vth), 8.0); sc[3] = a / c; }
-    else sc[slot] = a / (double)n;
+    if (OP == 0) sc[slot] = A;
+    else if (OP == 1) { sc[2] = thr2; sc[3] = A / C; }
+    else sc[slot] = A / (double)n;
+    *counter = 0u;
 }
 
 // vx[d > thr] /= d[d > thr], thr = max(raw density) / vth  (deposit.py:183-184)
@@ -155,12 +159,16 @@ sg_axis(FieldSet fs, int nx, int nz, int w, const double *__restrict__ coef,
 }
 
 // col[j] = sum_i (dx_i * (d[i+1][j] + d[i][j])) / 2.0 (numpy.trapz along
-// axis 0).  A block covers 32 columns; warp w sums rows w, w + 8, ... of its
-// lane's column in order, then the 8 warp partials are added in order.
+// axis 0): a block covers 32 columns, warp w sums rows w, w + 8, ... of its
+// lane's column in order, then the 8 warp partials are added in order; the
+// last block to finish then forms the numpy pairwise sum dsum of
+// (dz_j * (col[j+1] + col[j])) / 2.0 into sc[0].
 __global__ void __launch_bounds__(256)
-trapz_columns(const double *__restrict__ d, int nx, int nz, const double *__restrict__ dxg,
-              double *__restrict__ col) {
+trapz_once(const double *__restrict__ d, int nx, int nz, const double *__restrict__ dxg,
+           const double *__restrict__ dzg, double *__restrict__ col, double *__restrict__ terms,
+           double *__restrict__ sc, unsigned int *__restrict__ counter) {
     __shared__ double part[8][33];
+    __shared__ bool last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j = blockIdx.x * 32 + lane;
     double acc = 0.0;
@@ -178,15 +186,19 @@ trapz_columns(const double *__restrict__ d, int nx, int nz, const double *__rest
         for (int w = 1; w < 8; ++w) s = __dadd_rn(s, part[w][lane]);
         col[j] = s;
     }
-}
-
-// dsum = numpy pairwise sum of (dz_j * (col[j+1] + col[j])) / 2.0
-__global__ void trapz_final(const double *__restrict__ col, int nz, const double *__restrict__ dzg,
-                            double *__restrict__ terms, double *__restrict__ sc) {
-    for (int j = threadIdx.x; j < nz - 1; j += blockDim.x)
-        terms[j] = __ddiv_rn(__dmul_rn(dzg[j], __dadd_rn(col[j + 1], col[j])), 2.0);
+    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) sc[0] = np_pairwise(terms, nz - 1);
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int k = threadIdx.x; k < nz - 1; k += blockDim.x)
+        terms[k] = __ddiv_rn(__dmul_rn(dzg[k], __dadd_rn(__ldcg(col + k + 1), __ldcg(col + k))), 2.0);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        sc[0] = np_pairwise(terms, nz - 1);
+        *counter = 0u;
+    }
 }
 
 // density /= dsum; vx[density <= thr] = 0   (deposit.py:201-204)
@@ -256,7 +268,7 @@ extern "C" size_t dfcsr_df_workspace_bytes(int nx, int nz) {
     const size_t cells = (size_t)nx * nz;
     // 6 temporary fields, column sums, trapz terms, reduction partials
     return 6 * align_up(cells * sizeof(double), 256) + 2 * align_up((size_t)nz * sizeof(double), 256) +
-           align_up(2 * RED_BLOCKS * sizeof(double), 256) + 512;
+           align_up(2 * RED_BLOCKS * sizeof(double), 256) + 256 + 512;
 }
 
 extern "C" int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, double *vx,
@@ -290,30 +302,28 @@ extern "C" int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, doub
     double *U0 = c.take<double>(cells), *U1 = c.take<double>(cells), *U2 = c.take<double>(cells);
     double *col = c.take<double>(nz), *terms = c.take<double>(nz);
     double *rpart = c.take<double>(2 * RED_BLOCKS);
+    unsigned int *counter = c.take<unsigned int>(64);   // completion counters, zero between uses
     const int n = (int)cells;
     const int tb = 256, nb = (n + tb - 1) / tb;
     const double vth = p->velocity_threshold;
 
     ScopedTiming tm("df_finalize", s);
-    reduce_partial<0><<<RED_BLOCKS, 256, 0, s>>>(density, nullptr, n, sc, vth, rpart);
-    reduce_final<0><<<1, 32, 0, s>>>(rpart, RED_BLOCKS, n, sc, 5, vth);
+    DFCSR_CUDA_TRY(cudaMemsetAsync(counter, 0, 64 * sizeof(unsigned int), s));
+    reduce_once<0><<<RED_BLOCKS, 256, 0, s>>>(density, nullptr, n, sc, vth, rpart, 5, counter);
     threshold_divide<<<nb, tb, 0, s>>>(density, vx, n, sc, vth);
     launch_sg(0, FieldSet{{density, vx}, {T0, T1}}, 2, nx, nz, p, s);
     launch_sg(1, FieldSet{{T0, T1}, {density, vx}}, 2, nx, nz, p, s);
-    trapz_columns<<<(nz + 31) / 32, 256, 0, s>>>(density, nx, nz, p->dxg, col);
-    trapz_final<<<1, 256, 0, s>>>(col, nz, p->dzg, terms, sc);
+    trapz_once<<<(nz + 31) / 32, 256, 0, s>>>(density, nx, nz, p->dxg, p->dzg, col, terms, sc,
+                                              counter + 16);
     normalize_fields<<<nb, tb, 0, s>>>(density, vx, n, sc);
     gradients<<<nb, tb, 0, s>>>(density, vx, nx, nz, p->gx, p->gz, p->gx_uniform, p->gx_dx,
                                 p->gz_uniform, p->gz_dx, U0, U1, U2);
     launch_sg(0, FieldSet{{U0, U1, U2}, {T0, T1, T2}}, 3, nx, nz, p, s);
     launch_sg(1, FieldSet{{T0, T1, T2}, {density_x, density_z, vx_x}}, 3, nx, nz, p, s);
-    reduce_partial<0><<<RED_BLOCKS, 256, 0, s>>>(density, nullptr, n, sc, vth, rpart);
-    reduce_final<0><<<1, 32, 0, s>>>(rpart, RED_BLOCKS, n, sc, 6, vth);
-    reduce_partial<1><<<RED_BLOCKS, 256, 0, s>>>(density, vx_x, n, sc, vth, rpart);
-    reduce_final<1><<<1, 32, 0, s>>>(rpart, RED_BLOCKS, n, sc, 3, vth);
+    reduce_once<0><<<RED_BLOCKS, 256, 0, s>>>(density, nullptr, n, sc, vth, rpart, 6, counter);
+    reduce_once<1><<<RED_BLOCKS, 256, 0, s>>>(density, vx_x, n, sc, vth, rpart, 3, counter);
     fill_vxx<<<nb, tb, 0, s>>>(density, vx_x, n, sc);
-    reduce_partial<2><<<RED_BLOCKS, 256, 0, s>>>(vx_x, nullptr, n, sc, vth, rpart);
-    reduce_final<2><<<1, 32, 0, s>>>(rpart, RED_BLOCKS, n, sc, 4, vth);
+    reduce_once<2><<<RED_BLOCKS, 256, 0, s>>>(vx_x, nullptr, n, sc, vth, rpart, 4, counter);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }
