@@ -36,9 +36,9 @@ __device__ __forceinline__ double block_max(double v, double *red) {
 // OP 2: sum(f).  Final values: OP 0 -> sc[slot] = max; OP 1 -> sc[2] = thr2,
 // sc[3] = sum / count (NaN when empty, like numpy.mean of an empty
 // selection); OP 2 -> sc[slot] = sum / n.
-// Single-launch form: every block writes its partial, the last block to
-// finish (completion counter, reset by that block) adds the partials in
-// block order - the same result as reduce_partial + reduce_final.
+// One launch: every block writes its partial, and the last block to finish
+// (completion counter, reset by that block) combines the partials in block
+// order, so the result does not depend on which block finishes last.
 template <int OP>
 __global__ void __launch_bounds__(256)
 reduce_once(const double *__restrict__ f, const double *__restrict__ g, int n,
