@@ -361,11 +361,11 @@ def gpu_arm(a):
                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
         if a.precision == "mixed":
             # DRAM bytes and FP32 operations per integrand point from the ncu
-            # capture in profiles/wake_mixed_integral_chicane_2e6.md (42.15 MB
-            # and 2.22 GFLOP for a launch of 4.01e7 integrand points), scaled
+            # capture in profiles/wake_mixed_integral_chicane_2e6.md (42.2 MB
+            # and 2.20 GFLOP for a launch of 4.01e7 integrand points), scaled
             # to this launch size
-            traffic = 42.15e6 / 4.01e7 * per_launch_pts
-            flops = 2.22e9 / 4.01e7 * per_launch_pts
+            traffic = 42.2e6 / 4.01e7 * per_launch_pts
+            flops = 2.20e9 / 4.01e7 * per_launch_pts
             fp32_peak = fma_peaks["fp32_tflops"]
             out["roofline"]["traffic"] = traffic
             out["roofline"]["dram_frac"] = traffic / (launch_ms * 1e-3) / 1e9 / hbm
@@ -373,8 +373,9 @@ def gpu_arm(a):
                 "achieved_tflops": flops / (launch_ms * 1e-3) / 1e12, "peak_tflops": fp32_peak,
                 "frac": flops / (launch_ms * 1e-3) / 1e12 / fp32_peak,
                 "peak_source": "measured FMA rate (peaks_measured)"}
-            out["roofline"]["binding"] = ("L1TEX throughput: 80.5 % of peak in ncu (16 x 16-byte "
-                                          "gathers + 8 x 16-byte shared loads per integrand point)")
+            out["roofline"]["binding"] = ("gather latency / L1TEX: eight 32-byte history cells per "
+                                          "integrand point from L1/L2 (L1TEX 68 % of peak, top stall "
+                                          "long_scoreboard, issue 49 % in ncu)")
     out["peaks_measured"] = fma_peaks
     out["gpu_launches"] = int(sum(launches.values()))
     out["kernel_launches_by_name"] = launches
