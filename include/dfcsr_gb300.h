@@ -232,6 +232,11 @@ typedef struct {
     const double *lattice_delta;/* mixed only, optional: [nsample][6] row     */
                                 /* differences lattice[k+1] - lattice[k]      */
                                 /* (last row 0), or NULL                      */
+    const float *lattice_dw;    /* mixed only, optional: [nsample][6][2] the  */
+                                /* table as double-word FP32 pairs (hi, lo =  */
+                                /* value - hi), with lattice_delta_dw: the    */
+                                /* geometry then runs in double-word FP32;    */
+    const float *lattice_delta_dw; /* NULL: FP64                               */
 } dfcsr_wake_job;
 
 /* Plain FP64 drop-in: reproduces the reference's IEEE operation order

@@ -63,6 +63,8 @@ def wake_job(tracker, lattice, position, sigma_z, sigma_x, slope0, mean_x, forma
     j.zbins, j.xbins = int(zbins), int(xbins)
     j.near_band = float(near_band)
     j.lattice_delta = lattice.device_deltas().data_ptr()
+    tdw, ddw = lattice.device_tables_dw()
+    j.lattice_dw, j.lattice_delta_dw = tdw.data_ptr(), ddw.data_ptr()
     return j
 
 

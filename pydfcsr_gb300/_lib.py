@@ -90,6 +90,7 @@ class WakeJob(ctypes.Structure):
         ("zbins", _c_int), ("xbins", _c_int),
         ("near_band", _c_double),
         ("lattice_delta", _p),
+        ("lattice_dw", _p), ("lattice_delta_dw", _p),
     ]
 
 

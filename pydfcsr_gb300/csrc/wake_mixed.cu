@@ -25,6 +25,7 @@
 //  * band kernel (FP64, optional): s' columns with |s' - s| < near_band are
 //    skipped by the integral kernel and evaluated with the FP64 integrand.
 //  * finalize kernel: adds the regions in the reference's order and scales.
+#include "dw.cuh"
 #include "wake_common.cuh"
 
 namespace dfcsr {
@@ -124,7 +125,93 @@ struct GeoShared {
     double lat_s[6];
     double vx_obs;
     int nreg, ok;
+    // double-word forms for the double-word column path
+    dw S0[WAKE_MAX_REGIONS], Sst[WAKE_MAX_REGIONS];   // s'(j) = S0 + j Sst
+    dw U0[WAKE_MAX_REGIONS], Ust[WAKE_MAX_REGIONS];   // orbit-table coordinate of s'(j)
+    dw xrefw[WAKE_MAX_REGIONS];
+    dw Px, Py, T0, Tz, inv_t, inv_z, vxo, vyo, nsx, nsy, Sw;
 };
+
+__device__ __forceinline__ int cell_of(float fl, bool nan) {
+    if (nan) return 2000000000;
+    const int c = __float2int_rz(fl);   // integral; saturates for huge values
+    return max(min(c, 2000000000), -2000000000);
+}
+
+__device__ __forceinline__ bool dw_isnan(dw a) { return a.hi != a.hi; }
+
+// One s' column record in double-word FP32: the same quantities as the FP64
+// column code in mixed_geometry, from the double-word orbit tables.
+__device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared &gs, int r, int j,
+                                       float4 *o) {
+    const float fj = (float)j;
+    const dw spj = dw_add(gs.S0[r], dw_mul_f(gs.Sst[r], fj));
+    const dw u = dw_add(gs.U0[r], dw_mul_f(gs.Ust[r], fj));
+    dw L[6];
+    // interpolate1D rule: in range iff -1 < u < n; lower index int(u)
+    // (truncation: u in (-1, 0) uses index 0 and extrapolates)
+    const float fn = (float)J.nsample;
+    const bool gt = u.hi > -1.f || (u.hi == -1.f && u.lo > 0.f);
+    const bool lt = u.hi < fn || (u.hi == fn && u.lo < 0.f);
+    if (gt && lt) {
+        int a0 = (int)dw_floor(u);
+        if (a0 < 0) a0 = 0;
+        if (a0 > J.nsample - 1) a0 = J.nsample - 1;
+        const dw f = dw_add_f(u, -(float)a0);
+        const float2 *P = reinterpret_cast<const float2 *>(J.lattice_dw) + (size_t)a0 * 6;
+        const float2 *D = reinterpret_cast<const float2 *>(J.lattice_delta_dw) + (size_t)a0 * 6;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float2 p = P[k], d = D[k];
+            L[k] = dw_add(dw_make(p.x, p.y), dw_mul(f, dw_make(d.x, d.y)));
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) L[k] = dw_make(0.f, 0.f);
+    }
+    const dw npx = L[2], npy = L[3], tpx = L[4], tpy = L[5];
+    const dw xref = gs.xrefw[r];
+    const dw rx0 = dw_sub(dw_sub(gs.Px, L[0]), dw_mul(xref, npx));
+    const dw ry0 = dw_sub(dw_sub(gs.Py, L[1]), dw_mul(xref, npy));
+    const dw r0 = dw_sqrt(dw_add(dw_mul(rx0, rx0), dw_mul(ry0, ry0)));
+    const dw ut0 = dw_mul(dw_sub(gs.T0, r0), gs.inv_t);
+    const dw uz0 = dw_mul(dw_add(dw_sub(spj, gs.Tz), r0), gs.inv_z);
+    const float tfl = dw_floor(ut0), zfl = dw_floor(uz0);
+    const dw a = dw_add(dw_mul(gs.vxo, tpx), dw_mul(gs.vyo, tpy));
+    const dw bb = dw_add(dw_mul(gs.vxo, npx), dw_mul(gs.vyo, npy));
+    const dw e = dw_add(dw_mul(tpx, npx), dw_mul(tpy, npy));
+    const dw g = dw_add(dw_mul(npx, npx), dw_mul(npy, npy));
+    const dw h = dw_add(dw_mul(tpx, tpx), dw_mul(tpy, tpy));
+    const dw nmx = dw_sub(gs.nsx, npx), nmy = dw_sub(gs.nsy, npy);
+    const dw Q0 = dw_add(dw_mul(rx0, nmx), dw_mul(ry0, nmy));
+    const dw q2 = dw_add(dw_mul(gs.nsx, tpx), dw_mul(gs.nsy, tpy));
+    const dw ae = dw_mul(a, e);
+    float rho_f;
+    if (gs.nthr[r] >= 0) {
+        int el = gs.e_first[r];
+        for (int q = 0; q < gs.nthr[r]; ++q) el += (j >= gs.thr_j[r][q]) ? 1 : 0;
+        rho_f = (el < J.nelement) ? (float)J.rho[el] : 0.f;
+    } else {
+        rho_f = (float)rho_at(J, dw_to_double(spj));
+    }
+    const bool near = J.near_band > 0.0 && fabsf(dw_float(dw_sub(spj, gs.Sw))) < (float)J.near_band;
+    const Axis &ax_s = gs.ax_s[r];
+    const float ws = (j == 0 || j == ax_s.n - 1) ? (float)(0.5 * ax_s.step) : (float)ax_s.step;
+    o[0] = make_float4(__int_as_float(cell_of(tfl, dw_isnan(ut0))),
+                       __int_as_float(cell_of(zfl, dw_isnan(uz0))),
+                       dw_float(dw_add_f(ut0, -tfl)), dw_float(dw_add_f(uz0, -zfl)));
+    o[1] = make_float4(dw_float(r0), dw_float(dw_add(dw_mul(rx0, npx), dw_mul(ry0, npy))),
+                       dw_float(dw_add_f(g, -1.f)), rho_f);
+    o[2] = make_float4(dw_float(a), dw_float(bb), dw_float(e), dw_float(g));
+    o[3] = make_float4(dw_float(h), dw_float(dw_sub(bb, ae)),
+                       dw_float(dw_add(dw_add_f(dw_mul(a, g), -1.f), dw_mul(bb, e))),
+                       dw_float(dw_mul(bb, g)));
+    o[4] = make_float4(dw_float(dw_mul(a, dw_add_f(dw_neg(h), 1.f))), dw_float(dw_add(ae, dw_mul(bb, h))),
+                       dw_float(dw_mul(bb, e)), dw_float(Q0));
+    o[5] = make_float4(dw_float(dw_add(dw_mul(npx, nmx), dw_mul(npy, nmy))), dw_float(q2),
+                       dw_float(dw_sub(Q0, dw_mul(q2, r0))),
+                       near ? 0.f : (ax_s.n < 2 ? 0.f : ws));   // band columns: FP64 kernel
+}
 
 // One CTA per observation point: the per-point constants (regions, orbit at
 // s, vx at the observer) once in thread 0, then the s' columns of all regions
@@ -203,10 +290,34 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
             }
             gs.e_first[r] = ef;
             gs.nthr[r] = nb;
+            const double inv_s = 1.0 / J.s_delta;
+            gs.S0[r] = dw_from(A.start);
+            gs.Sst[r] = dw_from(A.step);
+            gs.U0[r] = dw_from((A.start - J.s_min) * inv_s);
+            gs.Ust[r] = dw_from(A.step * inv_s);
+            gs.xrefw[r] = dw_from(gs.xref[r]);
         }
     }
     __syncthreads();
     if (!gs.ok) return;
+    const bool use_dw = J.lattice_dw != nullptr && J.lattice_delta_dw != nullptr;
+    if (use_dw) {
+        if (threadIdx.x == 0) {
+            const double nx_ = gs.lat_s[2], ny_ = gs.lat_s[3];
+            gs.Px = dw_from(fma(x, nx_, gs.lat_s[0]));
+            gs.Py = dw_from(fma(x, ny_, gs.lat_s[1]));
+            gs.T0 = dw_from(t - J.t_min);
+            gs.Tz = dw_from(t + J.z_min);
+            gs.inv_t = dw_from(1.0 / J.t_delta);
+            gs.inv_z = dw_from(1.0 / J.z_delta);
+            gs.vxo = dw_from(gs.lat_s[4] + gs.vx_obs * nx_);
+            gs.vyo = dw_from(gs.lat_s[5] + gs.vx_obs * ny_);
+            gs.nsx = dw_from(nx_);
+            gs.nsy = dw_from(ny_);
+            gs.Sw = dw_from(s);
+        }
+        __syncthreads();
+    }
     const double X0s = gs.lat_s[0], Y0s = gs.lat_s[1], nsx = gs.lat_s[2], nsy = gs.lat_s[3];
     const double vxo = gs.lat_s[4] + gs.vx_obs * nsx, vyo = gs.lat_s[5] + gs.vx_obs * nsy;
     const double inv_s = 1.0 / J.s_delta, inv_t = 1.0 / J.t_delta, inv_z = 1.0 / J.z_delta;
@@ -222,6 +333,11 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         int r = 0;
         while (r + 1 < nreg && c >= gs.col_begin[r + 1]) ++r;
         const int j = c - gs.col_begin[r];
+        if (use_dw) {
+            float4 *o = reinterpret_cast<float4 *>(prec + gs.rm[r].col_off) + (size_t)j * (CW / 4);
+            column_dw(J, gs, r, j, o);
+            continue;
+        }
         const Axis ax_s = gs.ax_s[r];
         const double xref = gs.xref[r];
         const double spj = ax_s.at(j);

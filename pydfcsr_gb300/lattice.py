@@ -144,6 +144,26 @@ class Lattice:
             self._dev_delta = torch.from_numpy(np.ascontiguousarray(d)).to(dev)
         return self._dev_delta
 
+    def device_tables_dw(self):
+        """(table, row differences) as [Nsample, 6, 2] float32 CUDA tensors of
+        double-word pairs (hi, lo), cached: the mixed wake's geometry runs in
+        double-word FP32 from these."""
+        if getattr(self, "_dev_dw", None) is None:
+            tab = np.concatenate([self.coords, self.n_vec, self.tau_vec], axis=1)
+            d = np.zeros_like(tab)
+            d[:-1] = tab[1:] - tab[:-1]
+            dev = torch.device("cuda", torch.cuda.current_device())
+            self._dev_dw = (torch.from_numpy(_double_word(tab)).to(dev),
+                            torch.from_numpy(_double_word(d)).to(dev))
+        return self._dev_dw
+
+
+def _double_word(a):
+    """float32 pairs (hi, lo) with hi + lo the float64 value to ~48 bits."""
+    hi = a.astype(np.float32)
+    lo = (a - hi.astype(np.float64)).astype(np.float32)
+    return np.ascontiguousarray(np.stack([hi, lo], axis=-1))
+
 
 def _read_yaml(path):
     try:
