@@ -217,7 +217,7 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
 // s, vx at the observer) once in thread 0, then the s' columns of all regions
 // as one flat range across the block (full warps for the FP64 work), then
 // the x' rows likewise.
-__global__ void __launch_bounds__(GEO_THREADS)
+__global__ void __launch_bounds__(GEO_THREADS, 3)
 mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
                const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
                size_t rec_words, float *__restrict__ rec, PointMeta *__restrict__ meta,
