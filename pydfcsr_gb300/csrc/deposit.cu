@@ -8,7 +8,7 @@
 // the fractional offsets), and a gather pass forms the four corner sums that
 // land on each output cell.  Same result for the same input on every run; no
 // floating-point atomics anywhere.  GB300 runs FP64 at 1/64 of the FP32 rate,
-// so the per-particle FP64 work is kept to 6 (keys) + 13 (sums) operations.
+// so the per-particle FP64 work is kept to 6 (keys) + 10 (sums) operations.
 #include "dfcsr_common.cuh"
 
 namespace dfcsr {
@@ -314,16 +314,19 @@ static_assert(2 * (SEG_TILE + SEG_TILE / SEG_K) * 4 <= 48 * 1024, "seg_sums tile
 // weight channel: [sum w, sum w f1, sum w f2, sum w f1 f2].  The CIC corner
 // weights (1 - f1)(1 - f2), (1 - f1) f2, f1 (1 - f2), f1 f2 are linear in
 // these, so cic_assemble forms the corner sums from the moments.  Per
-// particle: 6 FP64 operations for f1, f2 and 3 + 4 for the two channels
-// (channel 0 without weights counts particles as an integer).
+// particle: 2 FP64 operations for f1, f2, one for f1 f2, and 3 + 4 for the
+// two channels (channel 0 without weights counts particles as an integer).
 template <bool W0, bool W1>
-__device__ __forceinline__ void cell_accumulate(uint32_t idx, double fi1, double fi2,
+__device__ __forceinline__ void cell_accumulate(uint32_t idx, double c1, double c2,
                                                 const double *__restrict__ q1, const double *__restrict__ q2,
                                                 const double *__restrict__ w0, const double *__restrict__ w1,
-                                                double start1, double inv1, double start2, double inv2,
-                                                double acc[8]) {
-    const double f1 = __dsub_rn(__dmul_rn(__dsub_rn(q1[idx], start1), inv1), fi1);
-    const double f2 = __dsub_rn(__dmul_rn(__dsub_rn(q2[idx], start2), inv2), fi2);
+                                                double inv1, double inv2, double acc[8]) {
+    // f = (q - start) inv - i as one FMA, q inv - (start inv + i), with the
+    // run constant c = start inv + i: the offset within the lower cell to
+    // ~1e-13 (it may step a hair outside [0, 1) at a cell edge, where the
+    // corner weights are continuous)
+    const double f1 = __fma_rn(q1[idx], inv1, -c1);
+    const double f2 = __fma_rn(q2[idx], inv2, -c2);
     const double p = __dmul_rn(f1, f2);
     if (W0) {
         const double w = w0[idx];
@@ -383,16 +386,17 @@ seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, i
     // so the FP64 work runs on full warps; only the flush at the end of a
     // run (integer work and stores) diverges.
     uint32_t k = m > 0 ? sk[seg_slot(off)] : nkeys;
-    double fi1 = (double)((int)(k / (uint32_t)(nb2 + 1)) - 1);
-    double fi2 = (double)((int)(k % (uint32_t)(nb2 + 1)) - 1);
+    const double s1i = __dmul_rn(start1, inv1), s2i = __dmul_rn(start2, inv2);
+    double fi1 = __dadd_rn(s1i, (double)((int)(k / (uint32_t)(nb2 + 1)) - 1));
+    double fi2 = __dadd_rn(s2i, (double)((int)(k % (uint32_t)(nb2 + 1)) - 1));
     double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int j0 = 0;
 #pragma unroll 1
     for (int j = 0; j < SEG_K; ++j) {
         const bool live = j < m && k < nkeys;      // outside-grid particles sort last
         if (live)
-            cell_accumulate<W0, W1>(sv[seg_slot(off + j)], fi1, fi2, q1, q2, w0, w1, start1, inv1,
-                                    start2, inv2, acc);
+            cell_accumulate<W0, W1>(sv[seg_slot(off + j)], fi1, fi2, q1, q2, w0, w1, inv1, inv2,
+                                    acc);
         const uint32_t kn = (j + 1 < m) ? sk[seg_slot(off + j + 1)] : 0xffffffffu;
         if (live && kn != k) {                     // the run of key k ends at j
             if (!W0) acc[0] = (double)(j + 1 - j0);
@@ -405,8 +409,8 @@ seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, i
             j0 = j + 1;
             k = kn;
             if (k < nkeys) {
-                fi1 = (double)((int)(k / (uint32_t)(nb2 + 1)) - 1);
-                fi2 = (double)((int)(k % (uint32_t)(nb2 + 1)) - 1);
+                fi1 = __dadd_rn(s1i, (double)((int)(k / (uint32_t)(nb2 + 1)) - 1));
+                fi2 = __dadd_rn(s2i, (double)((int)(k % (uint32_t)(nb2 + 1)) - 1));
             }
         }
     }
