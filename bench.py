@@ -28,7 +28,6 @@ GPU host) on the same config and prints the same metric.
 """
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys

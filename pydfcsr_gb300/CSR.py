@@ -18,8 +18,6 @@ one GPU and runs the same path.
 with the reference); ``'mixed'`` - FP32 bulk with FP64 retarded geometry;
 ``'both'`` keeps both history rings so either can be called.
 """
-import ctypes
-
 import numpy as np
 import torch
 

@@ -9,7 +9,6 @@ tau = (cos th, sin th) with th the accumulated bend angle.  The recursion
 (each sample built from the previous one) is kept as is: the wake reproduces
 the reference's linear interpolation of these exact tables.
 """
-import math
 from collections import OrderedDict
 
 import numpy as np

@@ -1,11 +1,10 @@
 """Shared test helpers: fixture loading and the oracle step driver."""
 import os
-from types import SimpleNamespace
 
 import numpy as np
 
 from oracle import oracle as O
-from pydfcsr_gb300.synthetic import StepPlan, dipole_lattice, chicane_lattice
+from pydfcsr_gb300.synthetic import StepPlan
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 

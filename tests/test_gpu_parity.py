@@ -268,7 +268,6 @@ def test_rgi_axis_tables_on_device_equal_host():
     """dfcsr_rgi_axis_linspace == the RegularGridInterpolator tables computed
     from the numpy linspace arrays (bit for bit), including targets outside
     the source grid on both sides and targets on source points."""
-    import ctypes
     from pydfcsr_gb300 import _lib
     from pydfcsr_gb300.coeffs import rgi_axis
     from pydfcsr_gb300.runtime import ptr, stream_handle
