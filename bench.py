@@ -224,6 +224,29 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True, side
             events.append(ev)
 
 
+def tracking_steps(run, first, count, precision, step_size):
+    """The reference's run loop with the CSR kick applied (CSR.py:297-334):
+    transport by the step's matrix and beam statistics, the DF step, the wake
+    on the mesh, Beam.apply_wakes (pz and px kicks) - every step depends on
+    the previous wake, so nothing overlaps across steps."""
+    import torch
+    from pydfcsr_gb300.runtime import as_device_f64
+    csr, beam = run.csr, run.beam
+    for k in range(first, first + count):
+        beam.track(run.plan.matrix(k), 0.0)
+        beam.position = float(run.plan.positions[k])
+        csr.update_history(run.plan.formation_length(k, beam.sigma_z))
+        csr.get_CSR_mesh()
+        s, x = csr.mesh_device()
+        dE, xk = csr.wake_device(s, x, precision)
+        xb, zb = int(csr.CSR_params.xbins), int(csr.CSR_params.zbins)
+        x0, x1, _, z0, z1, _, _, _, _ = csr._mesh
+        xr = as_device_f64(np.linspace(x0, x1, xb))
+        zr = as_device_f64(np.linspace(z0, z1, zb))
+        beam.apply_wakes(dE.view(xb, zb), xk.view(xb, zb), xr, zr, step_size, True, update=False)
+        run.last = (dE, xk)
+
+
 def e2e_steps(run, host_sets, first, count, precision, dev_bufs, side):
     """Steps through the public API with host buffers: H2D of (x, px, z)
     from pinned memory, CSR2D calls, D2H of (dE_dct, x_kick).
@@ -424,6 +447,25 @@ def gpu_arm(a):
                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                       "ms_per_step": e2e_s * 1000 / K}
         del re2e, host_sets
+
+    # the full tracking step with the kick fed back (no overlap possible)
+    if not a.no_e2e:
+        rtr, _ = make_run(wl, lattice, a.precision, seed_offset=beam_seed(rank))
+        step = float(lattice["step_size"])
+        tracking_steps(rtr, 1, W, a.precision, step)
+        barrier()
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        tracking_steps(rtr, W + 1, K, a.precision, step)
+        q1.record(stream)
+        barrier()
+        ms_tr = max_over_ranks(q0.elapsed_time(q1) / K, world, "cuda")
+        out["tracking_with_kicks"] = {
+            "value": job_value(npts, world, ms_tr), "unit": UNIT, "ms_per_step": ms_tr,
+            "definition": "Beam.track (transport kernel + statistics), get_DF / history, mesh, "
+                          "wake, Beam.apply_wakes with the wake (pz and px kicks) every step: the "
+                          "reference's run loop with apply_CSR; particles stay on the device"}
+        del rtr
 
     if a.serve_requests > 0 and a.precision == "mixed":
         out["serving"] = serving_leg(a.serve_requests, a.serve_rate, a.serve_fp64_sample,

@@ -103,9 +103,11 @@ class Beam:
             self.step += 1
         self.update_status()
 
-    def apply_wakes(self, dE_dct, x_kick, xrange, zrange, step_size, transverse_on):
+    def apply_wakes(self, dE_dct, x_kick, xrange, zrange, step_size, transverse_on, update=True):
         """Kick pz (and px when ``transverse_on``) by the wake interpolated at
-        (x_transform, z) (beams.py:108-131); updates the statistics."""
+        (x_transform, z) (beams.py:108-131); updates the statistics
+        (``update=False``, an extension: skip that when the caller tracks the
+        beam next, which updates them anyway)."""
         self._own()
         dE = as_device_f64(dE_dct)
         xk = as_device_f64(x_kick) if transverse_on else None
@@ -120,7 +122,8 @@ class Beam:
                   ptr(xk), ptr(xr), ptr(zr), nx, nz, float(self._slope[0]), float(self._slope[1]),
                   float(step_size), self._init_energy, 1 if transverse_on else 0, ptr(ws),
                   ws.numel(), stream_handle())
-        self.update_status()
+        if update:
+            self.update_status()
 
     @property
     def n_particle(self):

@@ -5,10 +5,9 @@ wake path - transport, get_DF, append_DF, append_interpolant,
 build_interpolant, get_CSR_mesh, calculate_2D_CSR - with r_gen6 linear
 transport in place of bmadx.  ``host_transport=True`` transports on the host
 in FP64 numpy (bit-identical particles to a CPU run of the same plan);
-otherwise the 6x6 matrices are applied on the device.
+otherwise the 6x6 matrices are applied on the device (dfcsr_transport6).
 """
 import numpy as np
-import torch
 
 from .beams import Beam
 from .CSR import CSR2D
@@ -39,8 +38,7 @@ class WakeRun:
             self.coords = self.plan.matrix(k) @ self.coords
             self.beam.set_coords(self.coords)
         else:
-            Rt = torch.as_tensor(self.plan.matrix(k), device=self.beam.particle.device)
-            self.beam.particle = (Rt @ self.beam.particle).contiguous()
+            self.beam.transport(self.plan.matrix(k))
             self.beam.update_status()
         self.beam.position = float(self.plan.positions[k])
         self.beam.step = k
