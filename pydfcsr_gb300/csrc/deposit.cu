@@ -10,7 +10,6 @@
 // floating-point atomics anywhere.  GB300 runs FP64 at 1/64 of the FP32 rate,
 // so the per-particle FP64 work is kept to 6 (keys) + 10 (sums) operations.
 #include "dfcsr_common.cuh"
-#include "dw.cuh"
 
 namespace dfcsr {
 
@@ -24,19 +23,13 @@ namespace dfcsr {
 //   pass 2: the |z| < 0.1 sigma_z slice (count, sum and square sum of
 //           x - mean_x) and x_transform = x - (slope z + intercept) (sum and
 //           square sum) -> sigma_x of the slice, mean and sigma of x_transform.
-// Per particle the FP64 pipe forms the shifted values (x - x0, or
-// x - (slope z + intercept)) and splits them into double-word FP32 pairs; the
-// per-thread sums run in double-word arithmetic (~1e-14 relative) and the
-// block and final reductions in FP64: 4 FP64 operations per particle in
-// pass 1 and 4-6 in pass 2.  The slice membership |z| < 0.1 sigma_z is an
-// exact FP64 comparison.
+// FP64 operations per particle: 7 in pass 1, 8 in pass 2.
 constexpr int MOM_THREADS = 256;
-constexpr int MOM_PER_THREAD = 32;
 constexpr int MOM_MAX_BLOCKS = 1024;
 constexpr int MOM_K = 5;   // partial sums per pass
 
 static int moment_blocks(int64_t n) {
-    int64_t b = (n + MOM_THREADS * MOM_PER_THREAD - 1) / (MOM_THREADS * MOM_PER_THREAD);
+    int64_t b = (n + MOM_THREADS * 8 - 1) / (MOM_THREADS * 8);
     if (b < 1) b = 1;
     if (b > MOM_MAX_BLOCKS) b = MOM_MAX_BLOCKS;
     return (int)b;
@@ -50,8 +43,7 @@ __global__ void __launch_bounds__(MOM_THREADS)
 moments_pass(const double *__restrict__ x, const double *__restrict__ z, int64_t n,
              const double *__restrict__ stats, double *__restrict__ partial) {
     __shared__ double red[MOM_THREADS / 32];
-    dw a1 = dw_make(0.f, 0.f), a2 = a1, a3 = a1, a4 = a1, a0 = a1;
-    int cnt = 0;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     double x0, z0, lim = 0, slope = 0, icpt = 0;
     if (PASS == 1) {
@@ -67,35 +59,25 @@ moments_pass(const double *__restrict__ x, const double *__restrict__ z, int64_t
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const double xi = x[i], zi = z[i];
         if (PASS == 1) {
-            const dw dx = dw_from(xi - x0), dz = dw_from(zi - z0);
-            a0 = dw_add(a0, dx);
-            a1 = dw_add(a1, dz);
-            a2 = dw_add(a2, dw_mul(dx, dx));
-            a3 = dw_add(a3, dw_mul(dz, dz));
-            a4 = dw_add(a4, dw_mul(dx, dz));
+            const double dx = xi - x0, dz = zi - z0;
+            a0 += dx;
+            a1 += dz;
+            a2 = fma(dx, dx, a2);
+            a3 = fma(dz, dz, a3);
+            a4 = fma(dx, dz, a4);
         } else {
             if (fabs(zi) < lim) {
-                const dw d = dw_from(xi - x0);
-                ++cnt;
-                a1 = dw_add(a1, d);
-                a2 = dw_add(a2, dw_mul(d, d));
+                const double d = xi - x0;
+                a0 += 1.0;
+                a1 += d;
+                a2 = fma(d, d, a2);
             }
-            const dw xt = dw_from(xi - fma(slope, zi, icpt));
-            a3 = dw_add(a3, xt);
-            a4 = dw_add(a4, dw_mul(xt, xt));
+            const double xt = xi - fma(slope, zi, icpt);
+            a3 += xt;
+            a4 = fma(xt, xt, a4);
         }
     }
-    double v[MOM_K];
-    if (PASS == 1) {
-        v[0] = dw_to_double(a0);
-        v[1] = dw_to_double(a1);
-    } else {
-        v[0] = (double)cnt;
-        v[1] = dw_to_double(a1);
-    }
-    v[2] = dw_to_double(a2);
-    v[3] = dw_to_double(a3);
-    v[4] = dw_to_double(a4);
+    double v[MOM_K] = {a0, a1, a2, a3, a4};
     for (int k = 0; k < MOM_K; ++k) {
         const double s = block_sum(v[k], red);
         if (threadIdx.x == 0) partial[(size_t)blockIdx.x * MOM_K + k] = s;
