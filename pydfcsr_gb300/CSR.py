@@ -15,7 +15,8 @@ observation mesh is one device call; ``parallel=True`` needs no MPI split on
 one GPU and runs the same path.
 
 ``precision``: ``'fp64'`` - plain FP64 drop-in (bit-compatible arithmetic
-with the reference); ``'mixed'`` - FP32 bulk with FP64 retarded geometry;
+with the reference); ``'mixed'`` - FP32 bulk with the retarded geometry in
+double-word FP32 (~48 bits);
 ``'both'`` keeps both history rings so either can be called.
 """
 import numpy as np
