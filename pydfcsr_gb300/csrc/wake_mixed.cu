@@ -1,9 +1,11 @@
-// Mixed-precision CSR wake (FP32 bulk, FP64 retarded geometry).
+// Mixed-precision CSR wake (FP32 bulk, retarded geometry at ~48 bits or more).
 //
 // Same integral as get_CSR_wake / get_CSR_integrand (pyDFCSR_2D/CSR.py:454-782),
 // restructured so that FP32 is safe and little work is wasted:
-//  * geometry kernel (FP64), one CTA per (observation point, region): per s'
-//    column the orbit tables at s', the separation R0 = r - r' at a reference
+//  * geometry kernel (double-word FP32 from the job's double-word orbit
+//    tables, ~48 bits; FP64 for jobs without them), one CTA per observation
+//    point: per s' column the orbit tables at s', the separation R0 = r - r'
+//    at a reference
 //    x' (the region centre), |R0|, the history coordinates of t_ret and
 //    s' - t_ret, and every direction product whose difference would cancel in
 //    FP32 (v.tau', v.n', 1 - |tau'|^2, |n'|^2 - 1, (r - r').(n - n'), ...);
