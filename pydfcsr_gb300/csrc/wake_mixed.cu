@@ -5,8 +5,7 @@
 //  * geometry kernel (double-word FP32 from the job's double-word orbit
 //    tables, ~48 bits; FP64 for jobs without them), one CTA per observation
 //    point: per s' column the orbit tables at s', the separation R0 = r - r'
-//    at a reference
-//    x' (the region centre), |R0|, the history coordinates of t_ret and
+//    at a reference x' (the region centre), |R0|, the history coordinates of t_ret and
 //    s' - t_ret, and every direction product whose difference would cancel in
 //    FP32 (v.tau', v.n', 1 - |tau'|^2, |n'|^2 - 1, (r - r').(n - n'), ...);
 //    per x' row the history x cell and the trapz weight, and the range of rows
