@@ -57,6 +57,7 @@ struct RegionMeta {
 
 struct PointMeta {
     int nreg, valid;
+    float inv_dt, inv_dz;   // FP32 reciprocals of the history t and z steps
     RegionMeta reg[WAKE_MAX_REGIONS];
 };
 
@@ -95,7 +96,7 @@ __device__ __forceinline__ Axis make_axis(double a, double b, int n) {
 }
 
 __device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *rm, bool &ok,
-                                       size_t rec_words) {
+                                       size_t rec_words, int max_rows) {
     int off = 0;
     ok = true;
     for (int k = 0; k < nreg; ++k) {
@@ -105,7 +106,7 @@ __device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *
         off += reg[k].nsp * CW;
         rm[k].row_off = off;
         off += reg[k].nxp * RW;
-        if (reg[k].nxp < 1 || reg[k].nxp > MX_MAX_ROWS || reg[k].nsp < 1 || reg[k].nsp > MX_MAX_COLS)
+        if (reg[k].nxp < 1 || reg[k].nxp > max_rows || reg[k].nsp < 1 || reg[k].nsp > MX_MAX_COLS)
             ok = false;
     }
     if ((size_t)off > rec_words) ok = false;
@@ -126,11 +127,18 @@ struct GeoShared {
     double lat_s[6];
     double vx_obs;
     int nreg, ok;
-    // double-word forms for the double-word column path
+    // double-word forms for the double-word column and row paths
     dw S0[WAKE_MAX_REGIONS], Sst[WAKE_MAX_REGIONS];   // s'(j) = S0 + j Sst
     dw U0[WAKE_MAX_REGIONS], Ust[WAKE_MAX_REGIONS];   // orbit-table coordinate of s'(j)
+    dw X0[WAKE_MAX_REGIONS], Xst[WAKE_MAX_REGIONS];   // x'(i) = X0 + i Xst
+    dw UX0[WAKE_MAX_REGIONS], UXst[WAKE_MAX_REGIONS]; // history x coordinate of x'(i)
     dw xrefw[WAKE_MAX_REGIONS];
-    dw Px, Py, T0, Tz, inv_t, inv_z, vxo, vyo, nsx, nsy, Sw;
+    dw Px, Py, T0, Tz, inv_t, inv_z, nsx, nsy, tsx, tsy, vxw, Sw;
+    // FP32 per-region constants: trapz weights (end point, inner point) in
+    // s' and x', curvature of the elements e_first + k, near band half-width
+    float wsf[WAKE_MAX_REGIONS][2], wxf[WAKE_MAX_REGIONS][2];
+    float rhof[WAKE_MAX_REGIONS][GEO_MAXB + 1];
+    float band_f;
 };
 
 __device__ __forceinline__ int cell_of(float fl, bool nan) {
@@ -144,7 +152,7 @@ __device__ __forceinline__ bool dw_isnan(dw a) { return a.hi != a.hi; }
 // One s' column record in double-word FP32: the same quantities as the FP64
 // column code in mixed_geometry, from the double-word orbit tables.
 __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared &gs, int r, int j,
-                                       float4 *o) {
+                                       dw vxo, dw vyo, float4 *o) {
     const float fj = (float)j;
     const dw spj = dw_add(gs.S0[r], dw_mul_f(gs.Sst[r], fj));
     const dw u = dw_add(gs.U0[r], dw_mul_f(gs.Ust[r], fj));
@@ -178,8 +186,8 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
     const dw ut0 = dw_mul(dw_sub(gs.T0, r0), gs.inv_t);
     const dw uz0 = dw_mul(dw_add(dw_sub(spj, gs.Tz), r0), gs.inv_z);
     const float tfl = dw_floor(ut0), zfl = dw_floor(uz0);
-    const dw a = dw_add(dw_mul(gs.vxo, tpx), dw_mul(gs.vyo, tpy));
-    const dw bb = dw_add(dw_mul(gs.vxo, npx), dw_mul(gs.vyo, npy));
+    const dw a = dw_add(dw_mul(vxo, tpx), dw_mul(vyo, tpy));
+    const dw bb = dw_add(dw_mul(vxo, npx), dw_mul(vyo, npy));
     const dw e = dw_add(dw_mul(tpx, npx), dw_mul(tpy, npy));
     const dw g = dw_add(dw_mul(npx, npx), dw_mul(npy, npy));
     const dw h = dw_add(dw_mul(tpx, tpx), dw_mul(tpy, tpy));
@@ -189,15 +197,14 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
     const dw ae = dw_mul(a, e);
     float rho_f;
     if (gs.nthr[r] >= 0) {
-        int el = gs.e_first[r];
-        for (int q = 0; q < gs.nthr[r]; ++q) el += (j >= gs.thr_j[r][q]) ? 1 : 0;
-        rho_f = (el < J.nelement) ? (float)J.rho[el] : 0.f;
+        int k = 0;
+        for (int q = 0; q < gs.nthr[r]; ++q) k += (j >= gs.thr_j[r][q]) ? 1 : 0;
+        rho_f = gs.rhof[r][k];
     } else {
         rho_f = (float)rho_at(J, dw_to_double(spj));
     }
-    const bool near = J.near_band > 0.0 && fabsf(dw_float(dw_sub(spj, gs.Sw))) < (float)J.near_band;
-    const Axis &ax_s = gs.ax_s[r];
-    const float ws = (j == 0 || j == ax_s.n - 1) ? (float)(0.5 * ax_s.step) : (float)ax_s.step;
+    const bool near = gs.band_f > 0.f && fabsf(dw_float(dw_sub(spj, gs.Sw))) < gs.band_f;
+    const float ws = (j == 0 || j == gs.ax_s[r].n - 1) ? gs.wsf[r][0] : gs.wsf[r][1];
     o[0] = make_float4(__int_as_float(cell_of(tfl, dw_isnan(ut0))),
                        __int_as_float(cell_of(zfl, dw_isnan(uz0))),
                        dw_float(dw_add_f(ut0, -tfl)), dw_float(dw_add_f(uz0, -zfl)));
@@ -211,114 +218,41 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
                        dw_float(dw_mul(bb, e)), dw_float(Q0));
     o[5] = make_float4(dw_float(dw_add(dw_mul(npx, nmx), dw_mul(npy, nmy))), dw_float(q2),
                        dw_float(dw_sub(Q0, dw_mul(q2, r0))),
-                       near ? 0.f : (ax_s.n < 2 ? 0.f : ws));   // band columns: FP64 kernel
+                       near ? 0.f : ws);   // band columns: FP64 kernel
 }
 
-// One CTA per observation point: the per-point constants (regions, orbit at
-// s, vx at the observer) once in thread 0, then the s' columns of all regions
-// as one flat range across the block (full warps for the FP64 work), then
-// the x' rows likewise.
-__global__ void __launch_bounds__(GEO_THREADS, 3)
-mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
-               const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
-               size_t rec_words, float *__restrict__ rec, PointMeta *__restrict__ meta,
-               int2 *__restrict__ rows_valid, double *__restrict__ obs_vx) {
-    __shared__ GeoShared gs;
-    const int64_t b = blockIdx.x;
-    const int64_t pt = first + b;
-    if (b >= count) return;
-    const dfcsr_wake_job &J = jobs[job_of_point ? job_of_point[pt] : 0];
-    const double t = J.position, s = S[pt], x = X[pt];
-    // the three independent per-point set-up tasks run in three warps
-    if (threadIdx.x == 32) {
-        gs.vx_obs = hist_field_fp64(J, 3, t, x, s - t);
-        obs_vx[b] = gs.vx_obs;
-    } else if (threadIdx.x == 64) {
-        lattice_lerp(J, s, gs.lat_s);
-    } else if (threadIdx.x < 32) {
-        // warp 0: lane 0 finds the regions and the record layout, then one
-        // lane per region sets up that region's axes and element thresholds
-        if (threadIdx.x == 0) {
-            gs.nreg = wake_regions(J, s, x, gs.reg);
-            bool ok;
-            layout(gs.reg, gs.nreg, gs.rm, ok, rec_words);
-            // the integral reads 32-byte cells with one 256-bit load: a ring
-            // that is not 32-byte aligned makes the point invalid (NaN result)
-            if (((uintptr_t)J.ring32 & 31u) != 0) ok = false;
-            gs.ok = ok ? 1 : 0;
-            PointMeta m;
-            m.nreg = gs.nreg;
-            m.valid = gs.ok;
-            for (int k = 0; k < WAKE_MAX_REGIONS; ++k)
-                m.reg[k] = (k < gs.nreg) ? gs.rm[k] : RegionMeta{0, 0, 0, 0};
-            meta[b] = m;
-            int cb = 0, rb = 0;
-            for (int r = 0; r < gs.nreg; ++r) {
-                gs.col_begin[r] = cb;
-                gs.row_begin[r] = rb;
-                cb += gs.reg[r].nsp;
-                rb += gs.reg[r].nxp;
-            }
-            gs.col_begin[gs.nreg] = cb;
-            gs.row_begin[gs.nreg] = rb;
-        }
-        __syncwarp();
-        const int r = threadIdx.x;
-        if (r < gs.nreg) {
-            const Region &R = gs.reg[r];
-            const Axis A = make_axis(R.sl, R.sr, R.nsp);
-            gs.ax_s[r] = A;
-            gs.ax_x[r] = make_axis(R.xl, R.xr, R.nxp);
-            gs.xref[r] = gs.ax_x[r].at(R.nxp / 2);
-            gs.lo[r] = R.nxp;
-            gs.hi[r] = -1;
-            // rho_at over the region's columns s'(j) = start + j step (non-
-            // decreasing in j): element index = number of element ends <= s'
-            const double s_first = A.at(0), s_last = A.at(R.nsp - 1);
-            int ef = 0, nb = (A.step > 0.0) ? 0 : -1;   // descending / flat: per column
-            for (int e = 0; e < J.nelement && nb >= 0; ++e) {
-                const double d = J.distance[e];
-                if (d <= s_first) ++ef;
-                else if (d <= s_last) {
-                    if (nb == GEO_MAXB) { nb = -1; break; }
-                    // first column j with s'(j) >= d
-                    int jj = (int)ceil((d - A.start) / A.step);
-                    jj = max(0, min(jj, R.nsp - 1));
-                    while (jj > 0 && A.at(jj - 1) >= d) --jj;
-                    while (jj < R.nsp - 1 && A.at(jj) < d) ++jj;
-                    gs.thr_j[r][nb++] = jj;
-                }
-            }
-            gs.e_first[r] = ef;
-            gs.nthr[r] = nb;
-            const double inv_s = 1.0 / J.s_delta;
-            gs.S0[r] = dw_from(A.start);
-            gs.Sst[r] = dw_from(A.step);
-            gs.U0[r] = dw_from((A.start - J.s_min) * inv_s);
-            gs.Ust[r] = dw_from(A.step * inv_s);
-            gs.xrefw[r] = dw_from(gs.xref[r]);
-        }
+// One x' row record in double-word FP32: history x cell with the reference's
+// rule (in range iff -1 < u < nx, lower index int(u), weight u - int(u)),
+// u = x' - x'_ref, x', trapz weight; in-range rows widen the valid range.
+__device__ __forceinline__ void row_dw(const dfcsr_wake_job &J, GeoShared &gs, int r, int i,
+                                       float4 *rb) {
+    const float fi = (float)i;
+    const dw ux = dw_add(gs.UX0[r], dw_mul_f(gs.UXst[r], fi));
+    const dw xpi = dw_add(gs.X0[r], dw_mul_f(gs.Xst[r], fi));
+    const float fnx = (float)J.nx;
+    const bool in = (ux.hi > -1.f || (ux.hi == -1.f && ux.lo > 0.f)) &&
+                    (ux.hi < fnx || (ux.hi == fnx && ux.lo < 0.f));
+    int x0 = 0, x1 = 0;
+    float xw = 0.f;
+    if (in) {
+        x0 = max((int)dw_floor(ux), 0);   // int() truncation: u in (-1, 0) -> 0
+        x1 = (x0 == J.nx - 1) ? x0 : x0 + 1;
+        xw = dw_float(dw_add_f(ux, -(float)x0));
     }
-    __syncthreads();
-    if (!gs.ok) return;
-    const bool use_dw = J.lattice_dw != nullptr && J.lattice_delta_dw != nullptr;
-    if (use_dw) {
-        if (threadIdx.x == 0) {
-            const double nx_ = gs.lat_s[2], ny_ = gs.lat_s[3];
-            gs.Px = dw_from(fma(x, nx_, gs.lat_s[0]));
-            gs.Py = dw_from(fma(x, ny_, gs.lat_s[1]));
-            gs.T0 = dw_from(t - J.t_min);
-            gs.Tz = dw_from(t + J.z_min);
-            gs.inv_t = dw_from(1.0 / J.t_delta);
-            gs.inv_z = dw_from(1.0 / J.z_delta);
-            gs.vxo = dw_from(gs.lat_s[4] + gs.vx_obs * nx_);
-            gs.vyo = dw_from(gs.lat_s[5] + gs.vx_obs * ny_);
-            gs.nsx = dw_from(nx_);
-            gs.nsy = dw_from(ny_);
-            gs.Sw = dw_from(s);
-        }
-        __syncthreads();
+    const int n = gs.ax_x[r].n;
+    rb[2 * i] = make_float4(__int_as_float(x0), xw, dw_float(dw_sub(xpi, gs.xrefw[r])), dw_float(xpi));
+    rb[2 * i + 1] = make_float4((i == 0 || i == n - 1) ? gs.wxf[r][0] : gs.wxf[r][1],
+                                __int_as_float(x1 - x0), 0.f, 0.f);
+    if (in) {
+        atomicMin(&gs.lo[r], i);   // integer min / max: order independent
+        atomicMax(&gs.hi[r], i);
     }
+}
+
+// FP64 column and row records (jobs without double-word orbit tables).
+__device__ __noinline__ void geometry_fp64(const dfcsr_wake_job &J, GeoShared &gs, double t, double s,
+                                           double x, float *prec, int ncols, int nrows) {
+    const int nreg = gs.nreg;
     const double X0s = gs.lat_s[0], Y0s = gs.lat_s[1], nsx = gs.lat_s[2], nsy = gs.lat_s[3];
     const double vxo = gs.lat_s[4] + gs.vx_obs * nsx, vyo = gs.lat_s[5] + gs.vx_obs * nsy;
     const double inv_s = 1.0 / J.s_delta, inv_t = 1.0 / J.t_delta, inv_z = 1.0 / J.z_delta;
@@ -326,19 +260,11 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
     // per-point constants: r(s) + x n(s), t - t_min, t + z_min
     const double Px = fma(x, nsx, X0s), Py = fma(x, nsy, Y0s);
     const double T0 = t - J.t_min, Tz = t + J.z_min;
-    const int nreg = gs.nreg;
-    float *prec = rec + (size_t)b * rec_words;
-    const int ncols = gs.col_begin[nreg];
     const double *dtab = J.lattice_delta;
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
         int r = 0;
         while (r + 1 < nreg && c >= gs.col_begin[r + 1]) ++r;
         const int j = c - gs.col_begin[r];
-        if (use_dw) {
-            float4 *o = reinterpret_cast<float4 *>(prec + gs.rm[r].col_off) + (size_t)j * (CW / 4);
-            column_dw(J, gs, r, j, o);
-            continue;
-        }
         const Axis ax_s = gs.ax_s[r];
         const double xref = gs.xref[r];
         const double spj = ax_s.at(j);
@@ -402,7 +328,6 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
                            near ? 0.f : (float)ax_s.weight(j));   // band columns: FP64 kernel
     }
     // rows: x cell, offset, u = x' - x'_ref, x', trapz weight; valid row range
-    const int nrows = gs.row_begin[nreg];
     for (int c = threadIdx.x; c < nrows; c += blockDim.x) {
         int r = 0;
         while (r + 1 < nreg && c >= gs.row_begin[r + 1]) ++r;
@@ -423,6 +348,154 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
             atomicMin(&gs.lo[r], i);   // integer min / max: order independent
             atomicMax(&gs.hi[r], i);
         }
+    }
+}
+
+// One CTA per observation point: the per-point constants (regions, orbit at
+// s, vx at the observer) once in thread 0, then the s' columns of all regions
+// as one flat range across the block (full warps for the FP64 work), then
+// the x' rows likewise.
+__global__ void __launch_bounds__(GEO_THREADS, 3)
+mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
+               const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
+               size_t rec_words, int max_rows, float *__restrict__ rec, PointMeta *__restrict__ meta,
+               int2 *__restrict__ rows_valid, double *__restrict__ obs_vx) {
+    __shared__ GeoShared gs;
+    const int64_t b = blockIdx.x;
+    const int64_t pt = first + b;
+    if (b >= count) return;
+    const dfcsr_wake_job &J = jobs[job_of_point ? job_of_point[pt] : 0];
+    const double t = J.position, s = S[pt], x = X[pt];
+    const bool use_dw = J.lattice_dw != nullptr && J.lattice_delta_dw != nullptr;
+    // the independent per-point set-up tasks run in separate warps
+    if (threadIdx.x == 32) {
+        gs.vx_obs = hist_field_fp64(J, 3, t, x, s - t);
+        obs_vx[b] = gs.vx_obs;
+        gs.vxw = dw_from(gs.vx_obs);
+    } else if (threadIdx.x == 64) {
+        lattice_lerp(J, s, gs.lat_s);
+        if (use_dw) {
+            const double nx_ = gs.lat_s[2], ny_ = gs.lat_s[3];
+            gs.Px = dw_from(fma(x, nx_, gs.lat_s[0]));
+            gs.Py = dw_from(fma(x, ny_, gs.lat_s[1]));
+            gs.nsx = dw_from(nx_);
+            gs.nsy = dw_from(ny_);
+            gs.tsx = dw_from(gs.lat_s[4]);
+            gs.tsy = dw_from(gs.lat_s[5]);
+        }
+    } else if (threadIdx.x == 96) {
+        if (use_dw) {
+            gs.T0 = dw_from(t - J.t_min);
+            gs.Tz = dw_from(t + J.z_min);
+            gs.inv_t = dw_from(1.0 / J.t_delta);
+            gs.inv_z = dw_from(1.0 / J.z_delta);
+            gs.Sw = dw_from(s);
+            gs.band_f = J.near_band > 0.0 ? (float)J.near_band : 0.f;
+        }
+    } else if (threadIdx.x < 32) {
+        // warp 0: lane 0 finds the regions and the record layout, then one
+        // lane per region sets up that region's axes and element thresholds
+        if (threadIdx.x == 0) {
+            gs.nreg = wake_regions(J, s, x, gs.reg);
+            bool ok;
+            layout(gs.reg, gs.nreg, gs.rm, ok, rec_words, max_rows);
+            // the integral reads 32-byte cells with one 256-bit load: a ring
+            // that is not 32-byte aligned makes the point invalid (NaN result)
+            if (((uintptr_t)J.ring32 & 31u) != 0) ok = false;
+            gs.ok = ok ? 1 : 0;
+            PointMeta m;
+            m.nreg = gs.nreg;
+            m.valid = gs.ok;
+            m.inv_dt = (float)(1.0 / J.t_delta);
+            m.inv_dz = (float)(1.0 / J.z_delta);
+            for (int k = 0; k < WAKE_MAX_REGIONS; ++k)
+                m.reg[k] = (k < gs.nreg) ? gs.rm[k] : RegionMeta{0, 0, 0, 0};
+            meta[b] = m;
+            int cb = 0, rb = 0;
+            for (int r = 0; r < gs.nreg; ++r) {
+                gs.col_begin[r] = cb;
+                gs.row_begin[r] = rb;
+                cb += gs.reg[r].nsp;
+                rb += gs.reg[r].nxp;
+            }
+            gs.col_begin[gs.nreg] = cb;
+            gs.row_begin[gs.nreg] = rb;
+        }
+        __syncwarp();
+        const int r = threadIdx.x;
+        if (r < gs.nreg) {
+            const Region &R = gs.reg[r];
+            const Axis A = make_axis(R.sl, R.sr, R.nsp);
+            const Axis AX = make_axis(R.xl, R.xr, R.nxp);
+            gs.ax_s[r] = A;
+            gs.ax_x[r] = AX;
+            gs.xref[r] = AX.at(R.nxp / 2);
+            gs.lo[r] = R.nxp;
+            gs.hi[r] = -1;
+            // rho_at over the region's columns s'(j) = start + j step (non-
+            // decreasing in j): element index = number of element ends <= s'
+            const double s_first = A.at(0), s_last = A.at(R.nsp - 1);
+            int ef = 0, nb = (A.step > 0.0) ? 0 : -1;   // descending / flat: per column
+            for (int e = 0; e < J.nelement && nb >= 0; ++e) {
+                const double d = J.distance[e];
+                if (d <= s_first) ++ef;
+                else if (d <= s_last) {
+                    if (nb == GEO_MAXB) { nb = -1; break; }
+                    // first column j with s'(j) >= d
+                    int jj = (int)ceil((d - A.start) / A.step);
+                    jj = max(0, min(jj, R.nsp - 1));
+                    while (jj > 0 && A.at(jj - 1) >= d) --jj;
+                    while (jj < R.nsp - 1 && A.at(jj) < d) ++jj;
+                    gs.thr_j[r][nb++] = jj;
+                }
+            }
+            gs.e_first[r] = ef;
+            gs.nthr[r] = nb;
+            for (int k = 0; k <= GEO_MAXB; ++k)
+                gs.rhof[r][k] = (k <= nb && ef + k < J.nelement) ? (float)J.rho[ef + k] : 0.f;
+            gs.wsf[r][0] = A.n < 2 ? 0.f : (float)(0.5 * A.step);
+            gs.wsf[r][1] = A.n < 2 ? 0.f : (float)A.step;
+            gs.wxf[r][0] = AX.n < 2 ? 0.f : (float)(0.5 * AX.step);
+            gs.wxf[r][1] = AX.n < 2 ? 0.f : (float)AX.step;
+            if (use_dw) {
+                const double inv_s = 1.0 / J.s_delta, inv_x = 1.0 / J.x_delta;
+                gs.S0[r] = dw_from(A.start);
+                gs.Sst[r] = dw_from(A.step);
+                gs.U0[r] = dw_from((A.start - J.s_min) * inv_s);
+                gs.Ust[r] = dw_from(A.step * inv_s);
+                gs.X0[r] = dw_from(AX.start);
+                gs.Xst[r] = dw_from(AX.step);
+                gs.UX0[r] = dw_from((AX.start - J.x_min) * inv_x);
+                gs.UXst[r] = dw_from(AX.step * inv_x);
+                gs.xrefw[r] = dw_from(gs.xref[r]);
+            }
+        }
+    }
+    __syncthreads();
+    if (!gs.ok) return;
+    const int nreg = gs.nreg;
+    float *prec = rec + (size_t)b * rec_words;
+    const int ncols = gs.col_begin[nreg];
+    const int nrows = gs.row_begin[nreg];
+    if (use_dw) {
+        // observer velocity direction v = tau(s) + vx n(s), FP32 double-word
+        const dw vxo = dw_add(gs.tsx, dw_mul(gs.vxw, gs.nsx));
+        const dw vyo = dw_add(gs.tsy, dw_mul(gs.vxw, gs.nsy));
+        for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+            int r = 0;
+            while (r + 1 < nreg && c >= gs.col_begin[r + 1]) ++r;
+            const int j = c - gs.col_begin[r];
+            float4 *o = reinterpret_cast<float4 *>(prec + gs.rm[r].col_off) + (size_t)j * (CW / 4);
+            column_dw(J, gs, r, j, vxo, vyo, o);
+        }
+        for (int c = threadIdx.x; c < nrows; c += blockDim.x) {
+            int r = 0;
+            while (r + 1 < nreg && c >= gs.row_begin[r + 1]) ++r;
+            const int i = c - gs.row_begin[r];
+            row_dw(J, gs, r, i, reinterpret_cast<float4 *>(prec + gs.rm[r].row_off));
+        }
+    } else {
+        geometry_fp64(J, gs, t, s, x, prec, ncols, nrows);
     }
     __syncthreads();
     if (threadIdx.x < nreg)
@@ -518,12 +591,46 @@ __device__ __forceinline__ void kahan(float &s, float &c, float v) {
     s = t;
 }
 
+// Shared memory of the integral kernel: the column records of one chunk, the
+// reduction slots and the point index, followed by the row records of one
+// region (2 * xbins_max rows, sized at launch so that the rest of the SM's
+// unified L1 / shared memory stays cache for the history gathers).
 struct IntegralSmem {
     float4 col[MX_CHUNK * CW / 4];
-    float4 row[MX_MAX_ROWS * RW / 4];
-    double red[MX_THREADS / 32];
+    float4 red[MX_THREADS / 32];
     long long pt;
 };
+constexpr size_t kIntegralRowOff = (sizeof(IntegralSmem) + 15) & ~(size_t)15;
+
+__host__ __device__ inline size_t integral_smem_bytes(int max_rows) {
+    return kIntegralRowOff + (size_t)max_rows * RW * sizeof(float);
+}
+
+// Deterministic block sum of two double-word values (fixed shuffle tree,
+// warps added in order by thread 0; result valid in thread 0).  FP32
+// double-word additions instead of FP64: GB300's FP64 rate is 1/72 of FP32.
+__device__ __forceinline__ void block_sum2_dw(dw &z, dw &x, float4 *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const dw oz{__shfl_down_sync(0xffffffffu, z.hi, o), __shfl_down_sync(0xffffffffu, z.lo, o)};
+        const dw ox{__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o)};
+        z = dw_add(z, oz);
+        x = dw_add(x, ox);
+    }
+    if (lane == 0) red[warp] = make_float4(z.hi, z.lo, x.hi, x.lo);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float4 r = red[0];
+        z = dw{r.x, r.y};
+        x = dw{r.z, r.w};
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            r = red[w];
+            z = dw_add(z, dw{r.x, r.y});
+            x = dw_add(x, dw{r.z, r.w});
+        }
+    }
+}
 
 struct RingView {
     const float4 *ring;
@@ -540,7 +647,8 @@ struct RingView {
 constexpr int MX_ROWBLK = 4;
 
 template <bool FF>
-__device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const RingView &V, int i_lo,
+__device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float4 *__restrict__ rows,
+                                             const RingView &V, int i_lo,
                                              int i_hi, int C, float &sz, float &cz, float &sx,
                                              float &cx) {
     const int nblk = (i_hi - i_lo + MX_ROWBLK - 1) / MX_ROWBLK;
@@ -562,7 +670,7 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const RingV
         const float4 g1 = cr[1], q2 = cr[2], q3 = cr[3], q4 = cr[4];
         const int iend = min(i0 + MX_ROWBLK, i_hi);
         for (int i = i0; i < iend; ++i) {
-            const float4 *rr = sm.row + i * (RW / 4);
+            const float4 *rr = rows + i * (RW / 4);
             const float4 ra = rr[0];
             const float4 rw = rr[1];
             const float wx = rw.x;
@@ -620,6 +728,7 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
                double *__restrict__ part, unsigned long long *__restrict__ counter) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     IntegralSmem &sm = *reinterpret_cast<IntegralSmem *>(smem_raw);
+    float4 *rows = reinterpret_cast<float4 *>(smem_raw + kIntegralRowOff);
     const int tid = threadIdx.x;
     for (;;) {
         if (tid == 0) sm.pt = (long long)atomicAdd(counter, 1ull);
@@ -627,20 +736,23 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         const int64_t b = sm.pt;
         if (b >= count) break;
         const dfcsr_wake_job &J = jobs[job_of_point ? job_of_point[first + b] : 0];
-        const PointMeta m = meta[b];
+        // PointMeta is read field by field: a local copy indexed by r would
+        // live in local memory
+        const PointMeta *m = meta + b;
         const float *base = rec + (size_t)b * rec_words;
         RingView V;
         V.ring = reinterpret_cast<const float4 *>(J.ring32);
         V.nt = J.nt; V.nx = J.nx; V.nz = J.nz; V.head = J.head; V.cap = J.cap;
-        V.inv_dt = (float)(1.0 / J.t_delta);
-        V.inv_dz = (float)(1.0 / J.z_delta);
-        for (int r = 0; r < m.nreg && m.valid; ++r) {
-            const RegionMeta R = m.reg[r];
+        V.inv_dt = m->inv_dt;
+        V.inv_dz = m->inv_dz;
+        const int nreg = m->valid ? m->nreg : 0;
+        for (int r = 0; r < nreg; ++r) {
+            const RegionMeta R = m->reg[r];
             const int2 rv = rows_valid[b * WAKE_MAX_REGIONS + r];
-            double reg_z = 0.0, reg_x = 0.0;
+            dw reg_z{0.f, 0.f}, reg_x{0.f, 0.f};
             if (rv.y > rv.x) {
                 const float4 *rb = reinterpret_cast<const float4 *>(base + R.row_off);
-                for (int k = tid; k < R.nxp * (RW / 4); k += blockDim.x) sm.row[k] = rb[k];
+                for (int k = tid; k < R.nxp * (RW / 4); k += blockDim.x) rows[k] = rb[k];
                 for (int j0 = 0; j0 < R.nsp; j0 += MX_CHUNK) {
                     const int C = min(MX_CHUNK, R.nsp - j0);
                     const float4 *cb = reinterpret_cast<const float4 *>(base + R.col_off) + (size_t)j0 * (CW / 4);
@@ -648,18 +760,19 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
                     __syncthreads();
                     float sz = 0.f, cz = 0.f, sx = 0.f, cx = 0.f;
                     if (r == 0)
-                        chunk_points<true>(sm, V, rv.x, rv.y, C, sz, cz, sx, cx);
+                        chunk_points<true>(sm, rows, V, rv.x, rv.y, C, sz, cz, sx, cx);
                     else
-                        chunk_points<false>(sm, V, rv.x, rv.y, C, sz, cz, sx, cx);
-                    const double bz = block_sum((double)sz - (double)cz, sm.red);
-                    const double bx = block_sum((double)sx - (double)cx, sm.red);
-                    if (tid == 0) { reg_z += bz; reg_x += bx; }
+                        chunk_points<false>(sm, rows, V, rv.x, rv.y, C, sz, cz, sx, cx);
+                    // Kahan state s - c exactly as a double-word
+                    dw bz = two_sum(sz, -cz), bx = two_sum(sx, -cx);
+                    block_sum2_dw(bz, bx, sm.red);
+                    if (tid == 0) { reg_z = dw_add(reg_z, bz); reg_x = dw_add(reg_x, bx); }
                     __syncthreads();
                 }
             }
             if (tid == 0) {
-                part[((size_t)b * WAKE_MAX_REGIONS + r) * 2 + 0] = reg_z;
-                part[((size_t)b * WAKE_MAX_REGIONS + r) * 2 + 1] = reg_x;
+                part[((size_t)b * WAKE_MAX_REGIONS + r) * 2 + 0] = dw_to_double(reg_z);
+                part[((size_t)b * WAKE_MAX_REGIONS + r) * 2 + 1] = dw_to_double(reg_x);
             }
         }
         __syncthreads();
@@ -676,9 +789,9 @@ mixed_band(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ 
     const int64_t b = blockIdx.x;
     const int r = blockIdx.y;
     if (b >= count) return;
-    const PointMeta m = meta[b];
+    const PointMeta *m = meta + b;
     double az = 0.0, ax = 0.0;
-    if (m.valid && r < m.nreg) {
+    if (m->valid && r < m->nreg) {
         const int64_t pt = first + b;
         const dfcsr_wake_job &J = jobs[job_of_point ? job_of_point[pt] : 0];
         if (J.near_band > 0.0) {
@@ -727,14 +840,14 @@ __global__ void mixed_finalize(const dfcsr_wake_job *__restrict__ jobs, const in
     if (b >= count) return;
     const int64_t pt = first + b;
     const dfcsr_wake_job &J = jobs[job_of_point ? job_of_point[pt] : 0];
-    const PointMeta m = meta[b];
-    if (!m.valid) {
+    const PointMeta *m = meta + b;
+    if (!m->valid) {
         dE[pt] = __longlong_as_double(0x7ff8000000000000ll);
         xkick[pt] = __longlong_as_double(0x7ff8000000000000ll);
         return;
     }
     double se = 0.0, sx = 0.0;
-    for (int r = 0; r < m.nreg; ++r) {
+    for (int r = 0; r < m->nreg; ++r) {
         const size_t k = ((size_t)b * WAKE_MAX_REGIONS + r) * 2;
         const double vz = part[k] + (band ? band[k] : 0.0);
         const double vx = part[k + 1] + (band ? band[k + 1] : 0.0);
@@ -779,14 +892,16 @@ static size_t mixed_carve(Carver &c, const MixedLayout &L, unsigned long long **
     return c.used;
 }
 
-static int integral_blocks() {
+static int integral_blocks(size_t smem) {
+    static size_t cached_smem = 0;
     static int cached = 0;
-    if (cached) return cached;
+    if (cached && cached_smem == smem) return cached;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mixed_integral, MX_THREADS,
-                                                      sizeof(IntegralSmem)) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mixed_integral, MX_THREADS, smem) !=
+            cudaSuccess || per_sm < 1)
         per_sm = 1;
     cached = per_sm * num_sms();
+    cached_smem = smem;
     return cached;
 }
 
@@ -834,22 +949,24 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
     static bool attr_set = false;
     if (!attr_set) {
         DFCSR_CUDA_TRY(cudaFuncSetAttribute(mixed_integral, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)sizeof(IntegralSmem)));
+                                            (int)integral_smem_bytes(MX_MAX_ROWS)));
         attr_set = true;
     }
-    const int blocks_max = integral_blocks();
+    const int max_rows = 2 * xbins_max;
+    const size_t smem = integral_smem_bytes(max_rows);
+    const int blocks_max = integral_blocks(smem);
     for (int64_t first = 0; first < n; first += L.batch) {
         const int64_t count = (n - first < L.batch) ? n - first : L.batch;
         DFCSR_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
         {
             ScopedTiming tm("wake_mixed_geometry", st);
             mixed_geometry<<<(unsigned)count, GEO_THREADS, 0, st>>>(
-                jobs, job_of_point, s, x, first, count, L.rec_words, rec, meta, rows, obs_vx);
+                jobs, job_of_point, s, x, first, count, L.rec_words, max_rows, rec, meta, rows, obs_vx);
         }
         const int blocks = (int)((int64_t)blocks_max < count ? blocks_max : count);
         {
             ScopedTiming tm("wake_mixed_integral", st);
-            mixed_integral<<<blocks, MX_THREADS, sizeof(IntegralSmem), st>>>(
+            mixed_integral<<<blocks, MX_THREADS, smem, st>>>(
                 jobs, job_of_point, first, count, L.rec_words, rec, meta, rows, part, counter);
         }
         if (use_band) {

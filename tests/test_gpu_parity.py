@@ -187,6 +187,35 @@ def test_wake_fp64_golden(tag):
 
 
 @cuda
+@pytest.mark.parametrize("tag", ["dipole", "chicane_pos"])
+def test_wake_mixed_geometry_paths(tag):
+    """The mixed kernel's two geometry paths on the same history: with the
+    double-word orbit tables (the default) and without them (FP64 geometry,
+    for C-ABI callers that leave the tables out).  Each is within 1e-4 of
+    the reference's mesh wake, and the two agree to 1e-6 of the peak."""
+    from pydfcsr_gb300.CSR import jobs_to_device
+    g = golden(f"wake_{tag}.npz")
+    run = _device_run_from_fixture(g)
+    csr = run.csr
+    csr.get_CSR_mesh()
+    s, x = csr.mesh_device()
+    ip = csr.integration_params
+    out = {}
+    for path in ("dw", "fp64"):
+        job = csr._job()
+        if path == "fp64":
+            job.lattice_dw = None
+            job.lattice_delta_dw = None
+        dE, xk = csr.evaluator.mixed(jobs_to_device([job]), s, x, ip.xbins, ip.zbins)
+        out[path] = (dE.cpu().numpy(), xk.cpu().numpy())
+    for path, (dE, xk) in out.items():
+        e = wake_errors(dE, xk, g["mesh_dE"], g["mesh_xkick"])
+        assert e["max_rel"] < 1e-4 and e["rms_rel"] < 1e-4, (path, e)
+    e = wake_errors(*out["fp64"], *out["dw"])
+    assert e["max_rel"] < 1e-6, e
+
+
+@cuda
 def test_wake_fp64_bitwise_on_oracle_history():
     """Same history, same beam statistics: the FP64 kernel reproduces the
     oracle (and so the reference) exactly."""
