@@ -199,18 +199,22 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True, side
     ``events`` (list) receives one (start, end) CUDA event pair per step.
 
     ``side``: a second stream for the beam moments.  The particle sets are
-    resident before the loop, so the moments of step k+1 need not wait for
-    the wake of step k on the main stream: the host gets them while the GPU
-    is still busy and enqueues step k+1 behind the wake without a gap."""
+    resident before the loop, so step k+1's moments are enqueued once step
+    k's mesh is built, ahead of step k's wake: they run beside step k's DF
+    kernels instead of queueing behind the wake's persistent blocks, and the
+    host has step k+1's statistics while the GPU is still busy with step k."""
     import torch
     csr = run.csr
     stream = torch.cuda.current_stream()
+    pre = None                      # step whose moments are already enqueued
     for k in range(first, first + count):
         if events is not None:
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record(stream)
-        run.beam.particle = sets[k - 1]
-        run.beam.update_status(stream=side)
+        if pre != k:
+            run.beam.particle = sets[k - 1]
+            run.beam.update_status(stream=side, wait=False)
+        run.beam.sync_status()
         run.beam.position = float(run.plan.positions[k])
         run.beam.step = k
         lf = run.plan.formation_length(k, run.beam.sigma_z)
@@ -218,6 +222,12 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True, side
         if wake:
             csr.get_CSR_mesh()
             s, x = csr.mesh_device()
+        if k + 1 < first + count:
+            # the wake job below takes step k's statistics (set at the sync)
+            run.beam.particle = sets[k]
+            run.beam.update_status(stream=side, wait=False)
+            pre = k + 1
+        if wake:
             run.last = csr.wake_device(s, x, precision)
         if events is not None:
             ev[1].record(stream)
@@ -251,17 +261,19 @@ def e2e_steps(run, host_sets, first, count, precision, dev_bufs, side):
     """Steps through the public API with host buffers: H2D of (x, px, z)
     from pinned memory, CSR2D calls, D2H of (dE_dct, x_kick).
 
-    Pipelined like a caller that streams beams through: step k+1's upload and
-    moments run on ``side`` into the other of two device buffers while step
-    k's wake runs on the main stream, and step k's results (calculate_2D_CSR
-    with wait=False) are read back after step k+1 is enqueued."""
+    Pipelined like a caller that streams beams through: once step k's mesh is
+    built, step k+1's upload and moments are enqueued on ``side`` into the
+    other of two device buffers, ahead of step k's wake on the main stream,
+    and step k's results (calculate_2D_CSR with wait=False) are read back
+    after step k+1 is enqueued."""
     import torch
     csr = run.csr
     main = torch.cuda.current_stream()
     h2d = d2h = 0
     used = [None, None]           # event: last read of each device buffer (get_DF)
-    pending = None
-    for k in range(first, first + count):
+    ready = [None, None]          # event: upload and moments of each buffer done
+
+    def upload(k):
         xpz = host_sets[k - 1]                      # pinned (3, N): x, px, z
         buf = dev_bufs[k % 2]
         with torch.cuda.stream(side):
@@ -270,15 +282,26 @@ def e2e_steps(run, host_sets, first, count, precision, dev_bufs, side):
             buf[0].copy_(xpz[0], non_blocking=True)
             buf[1].copy_(xpz[1], non_blocking=True)
             buf[4].copy_(xpz[2], non_blocking=True)
-        h2d += xpz.numel() * 8
         run.beam.particle = buf
-        run.beam.update_status(stream=side)
-        main.wait_event(side.record_event())
+        run.beam.update_status(stream=side, wait=False)
+        ready[k % 2] = side.record_event()
+        return xpz.numel() * 8
+
+    pending = None
+    pre = None                    # step whose upload is already enqueued
+    for k in range(first, first + count):
+        if pre != k:
+            h2d += upload(k)
+        run.beam.sync_status()
+        main.wait_event(ready[k % 2])
         run.beam.position = float(run.plan.positions[k])
         lf = run.plan.formation_length(k, run.beam.sigma_z)
         csr.update_history(lf)
         used[k % 2] = main.record_event()
         csr.get_CSR_mesh()
+        if k + 1 < first + count:
+            h2d += upload(k + 1)
+            pre = k + 1
         nxt = csr.calculate_2D_CSR(precision, wait=False)
         if pending is not None:
             dE, xk = pending.result()               # step k-1 on the host

@@ -35,7 +35,7 @@ constexpr int MX_THREADS = 256;
 constexpr int MX_CHUNK = 128;       // s' columns staged in shared memory at once
 constexpr int MX_MAX_ROWS = 1024;   // x' rows per region (2 * xbins)
 constexpr int MX_MAX_COLS = 4096;   // s' columns per region (zbins)
-constexpr int GEO_THREADS = 256;
+constexpr int GEO_THREADS = 128;
 constexpr int GEO_MAXB = 6;
 
 // Column record: 28 words (7 float4; stride 112 B keeps 8-lane phases of
@@ -351,11 +351,12 @@ __device__ __noinline__ void geometry_fp64(const dfcsr_wake_job &J, GeoShared &g
     }
 }
 
-// One CTA per observation point: the per-point constants (regions, orbit at
-// s, vx at the observer) once in thread 0, then the s' columns of all regions
-// as one flat range across the block (full warps for the FP64 work), then
-// the x' rows likewise.
-__global__ void __launch_bounds__(GEO_THREADS, 3)
+// One 128-thread CTA per observation point (six per SM, so that other CTAs'
+// column work covers one CTA's serial set-up): the per-point constants
+// (regions and record layout, orbit at s, vx at the observer, per-region
+// axes) by single threads of different warps, then the s' columns of all
+// regions as one flat range across the block, then the x' rows likewise.
+__global__ void __launch_bounds__(GEO_THREADS, 6)
 mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
                const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
                size_t rec_words, int max_rows, float *__restrict__ rec, PointMeta *__restrict__ meta,
