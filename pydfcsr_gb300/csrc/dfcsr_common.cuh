@@ -96,28 +96,60 @@ __device__ __forceinline__ double np_linspace_at(double start, double stop, int 
     return __dadd_rn(__dmul_rn((double)i, step), start);
 }
 
-// numpy pairwise summation (PW_BLOCKSIZE 128, 8 partial accumulators).
-__device__ inline double np_pairwise(const double *a, int n) {
+// numpy pairwise summation (PW_BLOCKSIZE 128, 8 partial accumulators):
+// blocks of at most 128 values summed with 8 accumulators ...
+__device__ inline double np_pairwise_block(const double *a, int n) {
     if (n < 8) {
         double r = (n > 0) ? a[0] : 0.0;
         for (int i = 1; i < n; ++i) r = __dadd_rn(r, a[i]);
         return r;
     }
-    if (n <= 128) {
-        double r[8];
-        for (int k = 0; k < 8; ++k) r[k] = a[k];
-        int i;
-        for (i = 8; i < n - (n % 8); i += 8)
-            for (int k = 0; k < 8; ++k) r[k] = __dadd_rn(r[k], a[i + k]);
-        double res = __dadd_rn(__dadd_rn(__dadd_rn(r[0], r[1]), __dadd_rn(r[2], r[3])),
-                               __dadd_rn(__dadd_rn(r[4], r[5]), __dadd_rn(r[6], r[7])));
-        for (; i < n; ++i) res = __dadd_rn(res, a[i]);
-        return res;
+    double r[8];
+    for (int k = 0; k < 8; ++k) r[k] = a[k];
+    int i;
+    for (i = 8; i < n - (n % 8); i += 8)
+        for (int k = 0; k < 8; ++k) r[k] = __dadd_rn(r[k], a[i + k]);
+    double res = __dadd_rn(__dadd_rn(__dadd_rn(r[0], r[1]), __dadd_rn(r[2], r[3])),
+                           __dadd_rn(__dadd_rn(r[4], r[5]), __dadd_rn(r[6], r[7])));
+    for (; i < n; ++i) res = __dadd_rn(res, a[i]);
+    return res;
+}
+
+// ... and longer runs split in halves (the first a multiple of 8), summed
+// left then right.  numpy recurses; this walks the same tree with an
+// explicit stack, so the frame is static (a recursive device function's
+// depth is not in the compiler's stack estimate).  A split at least halves
+// the length, so 31 levels cover any int n.
+__device__ inline double np_pairwise(const double *a, int n) {
+    if (n <= 128) return np_pairwise_block(a, n);
+    int off_s[32], len_s[32];
+    double left_s[32];
+    unsigned char st_s[32];
+    int sp = 0;
+    off_s[0] = 0; len_s[0] = n; st_s[0] = 0;
+    double ret = 0.0;
+    for (;;) {
+        const int off = off_s[sp], len = len_s[sp];
+        if (len <= 128) {
+            ret = np_pairwise_block(a + off, len);
+            --sp;   // the root is longer than 128, so sp >= 0 here
+            continue;
+        }
+        int n2 = len / 2;
+        n2 -= n2 % 8;
+        if (st_s[sp] == 0) {            // left half
+            st_s[sp] = 1;
+            ++sp; off_s[sp] = off; len_s[sp] = n2; st_s[sp] = 0;
+        } else if (st_s[sp] == 1) {     // right half
+            left_s[sp] = ret;
+            st_s[sp] = 2;
+            ++sp; off_s[sp] = off + n2; len_s[sp] = len - n2; st_s[sp] = 0;
+        } else {                        // both done
+            ret = __dadd_rn(left_s[sp], ret);
+            if (sp == 0) return ret;
+            --sp;
+        }
     }
-    // split in halves (multiple of 8) and recurse, as numpy does
-    int n2 = n / 2;
-    n2 -= n2 % 8;
-    return __dadd_rn(np_pairwise(a, n2), np_pairwise(a + n2, n - n2));
 }
 
 // Deterministic block reduction of a double (fixed shuffle tree + fixed
