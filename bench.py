@@ -334,8 +334,10 @@ def gpu_arm(a):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # warm-up (builds the history; untimed)
-    side = torch.cuda.Stream()
+    # warm-up (builds the history; untimed).  The side stream (next step's
+    # moments, uploads) has the highest priority: its blocks are scheduled as
+    # soon as an SM frees, rather than behind the queued wake blocks
+    side = torch.cuda.Stream(priority=-5)
     timed_steps(run, sets, 1, W, a.precision, side=side)
     barrier()
     fma_peaks = measure_fma_peaks()

@@ -84,26 +84,51 @@ __global__ void regrid5(const double *__restrict__ f0, const double *__restrict_
 // that are both numpy linspaces: i = clip(searchsorted(src, t, 'right') - 1,
 // 0, ns - 2), w = (t - src[i]) / (src[i+1] - src[i]), oob = t < src[0] or
 // t > src[ns-1].  Grid values are regenerated with numpy's linspace formula,
-// so the tables equal the ones computed from the host arrays.
+// so the tables equal the ones computed from the host arrays.  The interval
+// is guessed from (t - src[0]) / step and then corrected by exact
+// comparisons with the grid values (two or three steps instead of a binary
+// search: every FP64 operation here costs some hundred cycles of latency).
+struct Linspace {   // numpy.linspace(start, stop, num) element by element
+    double start, stop, delta, step;
+    int num;
+    __device__ Linspace(double a, double b, int n) : start(a), stop(b), num(n) {
+        const int div = n - 1;
+        delta = __dsub_rn(b, a);
+        step = div > 0 ? __ddiv_rn(delta, (double)div) : 0.0;
+    }
+    __device__ double at(int i) const {
+        if (num == 1) return start;
+        if (i == num - 1) return stop;
+        if (step == 0.0) return __dadd_rn(__dmul_rn(__ddiv_rn((double)i, (double)(num - 1)), delta), start);
+        return __dadd_rn(__dmul_rn((double)i, step), start);
+    }
+};
+
 __global__ void rgi_axis_linspace(double s0, double s1, int ns, double t0, double t1, int nt,
                                   int32_t *__restrict__ idx, double *__restrict__ w,
                                   uint8_t *__restrict__ oob) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nt) return;
-    const double t = np_linspace_at(t0, t1, nt, m);
-    int lo = 0, hi = ns;                      // count of src values <= t
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (np_linspace_at(s0, s1, ns, mid) <= t) lo = mid + 1;
-        else hi = mid;
+    const Linspace src(s0, s1, ns);
+    const double t = Linspace(t0, t1, nt).at(m);
+    // g = (number of source values <= t) - 1, from a guess within a step or
+    // two of it; NaN -> -1 (no value compares <= NaN)
+    int g = -1;
+    if (t == t) {
+        double gd = floor(__dmul_rn(__dsub_rn(t, s0), __drcp_rn(src.step)));
+        if (!(gd >= -1.0)) gd = -1.0;
+        if (gd > (double)(ns - 1)) gd = (double)(ns - 1);
+        g = (int)gd;
+        while (g + 1 < ns && src.at(g + 1) <= t) ++g;
+        while (g >= 0 && src.at(g) > t) --g;
     }
-    int i = lo - 1;
+    int i = g;
     if (i < 0) i = 0;
     if (i > ns - 2) i = ns - 2;
-    const double a = np_linspace_at(s0, s1, ns, i), b = np_linspace_at(s0, s1, ns, i + 1);
+    const double a = src.at(i), b = src.at(i + 1);
     idx[m] = i;
     w[m] = __ddiv_rn(__dsub_rn(t, a), __dsub_rn(b, a));
-    oob[m] = (t < np_linspace_at(s0, s1, ns, 0) || t > np_linspace_at(s0, s1, ns, ns - 1)) ? 1 : 0;
+    oob[m] = (t < src.at(0) || t > src.at(ns - 1)) ? 1 : 0;
 }
 
 }  // namespace dfcsr
