@@ -36,6 +36,7 @@ constexpr int MX_CHUNK = 128;       // s' columns staged in shared memory at onc
 constexpr int MX_MAX_ROWS = 1024;   // x' rows per region (2 * xbins)
 constexpr int MX_MAX_COLS = 4096;   // s' columns per region (zbins)
 constexpr int GEO_THREADS = 128;
+constexpr int SETUP_THREADS = 64;
 constexpr int GEO_MAXB = 6;
 
 // Column record: 28 words (7 float4; stride 112 B keeps 8-lane phases of
@@ -112,7 +113,7 @@ __device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *
     if ((size_t)off > rec_words) ok = false;
 }
 
-struct GeoShared {
+struct alignas(16) GeoShared {
     Region reg[WAKE_MAX_REGIONS];
     RegionMeta rm[WAKE_MAX_REGIONS];
     Axis ax_s[WAKE_MAX_REGIONS], ax_x[WAKE_MAX_REGIONS];
@@ -139,6 +140,7 @@ struct GeoShared {
     float wsf[WAKE_MAX_REGIONS][2], wxf[WAKE_MAX_REGIONS][2];
     float rhof[WAKE_MAX_REGIONS][GEO_MAXB + 1];
     float band_f;
+    float inv_dt_f, inv_dz_f;   // FP32 reciprocals of the history t and z steps
 };
 
 __device__ __forceinline__ int cell_of(float fl, bool nan) {
@@ -351,16 +353,19 @@ __device__ __noinline__ void geometry_fp64(const dfcsr_wake_job &J, GeoShared &g
     }
 }
 
-// One 128-thread CTA per observation point (six per SM, so that other CTAs'
-// column work covers one CTA's serial set-up): the per-point constants
-// (regions and record layout, orbit at s, vx at the observer, per-region
-// axes) by single threads of different warps, then the s' columns of all
-// regions as one flat range across the block, then the x' rows likewise.
-__global__ void __launch_bounds__(GEO_THREADS, 6)
-mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
-               const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
-               size_t rec_words, int max_rows, float *__restrict__ rec, PointMeta *__restrict__ meta,
-               int2 *__restrict__ rows_valid, double *__restrict__ obs_vx) {
+// Per-point set-up of the geometry: regions and record layout, orbit at s,
+// vx at the observer, per-region axes, element thresholds and double-word
+// constants.  These are chains of dependent FP64 operations (some hundred
+// cycles each on this GPU) done by single threads, so they run in a kernel
+// of their own: 64-thread CTAs, many per SM, hide one another's latency,
+// and the geometry CTAs start from the finished record.  Two warps: warp 0
+// finds the regions (lane 0) and sets up one region per lane; in warp 1,
+// lane 0 interpolates vx at the observer, lane 1 the orbit at s, lane 2 the
+// history constants.
+__global__ void __launch_bounds__(SETUP_THREADS)
+mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
+            const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
+            size_t rec_words, int max_rows, GeoShared *__restrict__ setup) {
     __shared__ GeoShared gs;
     const int64_t b = blockIdx.x;
     const int64_t pt = first + b;
@@ -371,9 +376,8 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
     // the independent per-point set-up tasks run in separate warps
     if (threadIdx.x == 32) {
         gs.vx_obs = hist_field_fp64(J, 3, t, x, s - t);
-        obs_vx[b] = gs.vx_obs;
         gs.vxw = dw_from(gs.vx_obs);
-    } else if (threadIdx.x == 64) {
+    } else if (threadIdx.x == 33) {
         lattice_lerp(J, s, gs.lat_s);
         if (use_dw) {
             const double nx_ = gs.lat_s[2], ny_ = gs.lat_s[3];
@@ -384,7 +388,7 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
             gs.tsx = dw_from(gs.lat_s[4]);
             gs.tsy = dw_from(gs.lat_s[5]);
         }
-    } else if (threadIdx.x == 96) {
+    } else if (threadIdx.x == 34) {
         if (use_dw) {
             gs.T0 = dw_from(t - J.t_min);
             gs.Tz = dw_from(t + J.z_min);
@@ -404,14 +408,8 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
             // that is not 32-byte aligned makes the point invalid (NaN result)
             if (((uintptr_t)J.ring32 & 31u) != 0) ok = false;
             gs.ok = ok ? 1 : 0;
-            PointMeta m;
-            m.nreg = gs.nreg;
-            m.valid = gs.ok;
-            m.inv_dt = (float)(1.0 / J.t_delta);
-            m.inv_dz = (float)(1.0 / J.z_delta);
-            for (int k = 0; k < WAKE_MAX_REGIONS; ++k)
-                m.reg[k] = (k < gs.nreg) ? gs.rm[k] : RegionMeta{0, 0, 0, 0};
-            meta[b] = m;
+            gs.inv_dt_f = (float)(1.0 / J.t_delta);
+            gs.inv_dz_f = (float)(1.0 / J.z_delta);
             int cb = 0, rb = 0;
             for (int r = 0; r < gs.nreg; ++r) {
                 gs.col_begin[r] = cb;
@@ -473,6 +471,44 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         }
     }
     __syncthreads();
+    // the finished record to global memory
+    const uint4 *src = reinterpret_cast<const uint4 *>(&gs);
+    uint4 *dst = reinterpret_cast<uint4 *>(setup + b);
+    for (int k = threadIdx.x; k < (int)(sizeof(GeoShared) / 16); k += blockDim.x) dst[k] = src[k];
+}
+
+// One 128-thread CTA per observation point (six per SM): the point's set-up
+// record from mixed_setup, then the s' columns of all regions as one flat
+// range across the block, then the x' rows likewise.
+__global__ void __launch_bounds__(GEO_THREADS, 6)
+mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
+               const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
+               const GeoShared *__restrict__ setup, size_t rec_words, float *__restrict__ rec,
+               PointMeta *__restrict__ meta, int2 *__restrict__ rows_valid, double *__restrict__ obs_vx) {
+    __shared__ GeoShared gs;
+    const int64_t b = blockIdx.x;
+    const int64_t pt = first + b;
+    if (b >= count) return;
+    const dfcsr_wake_job &J = jobs[job_of_point ? job_of_point[pt] : 0];
+    const double t = J.position, s = S[pt], x = X[pt];
+    const bool use_dw = J.lattice_dw != nullptr && J.lattice_delta_dw != nullptr;
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(setup + b);
+        uint4 *dst = reinterpret_cast<uint4 *>(&gs);
+        for (int k = threadIdx.x; k < (int)(sizeof(GeoShared) / 16); k += blockDim.x) dst[k] = src[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        PointMeta m;
+        m.nreg = gs.nreg;
+        m.valid = gs.ok;
+        m.inv_dt = gs.inv_dt_f;
+        m.inv_dz = gs.inv_dz_f;
+        for (int k = 0; k < WAKE_MAX_REGIONS; ++k)
+            m.reg[k] = (k < gs.nreg) ? gs.rm[k] : RegionMeta{0, 0, 0, 0};
+        meta[b] = m;
+        obs_vx[b] = gs.vx_obs;
+    }
     if (!gs.ok) return;
     const int nreg = gs.nreg;
     float *prec = rec + (size_t)b * rec_words;
@@ -863,7 +899,10 @@ __global__ void mixed_finalize(const dfcsr_wake_job *__restrict__ jobs, const in
 struct MixedLayout {
     size_t rec_words;
     int64_t batch;
+    int64_t setup_pts;   // points per set-up launch (a whole number of batches)
 };
+
+constexpr int SETUP_BATCHES = 4;
 
 static const size_t kMixedScratchTarget = (size_t)96 << 20;   // keep batches L2-sized
 
@@ -877,13 +916,15 @@ static MixedLayout mixed_layout(int xbins_max, int zbins_max, int64_t n) {
     if (batch < 1) batch = 1;
     if (batch > n) batch = n;
     L.batch = batch;
+    L.setup_pts = (n < SETUP_BATCHES * batch) ? n : SETUP_BATCHES * batch;
     return L;
 }
 
 static size_t mixed_carve(Carver &c, const MixedLayout &L, unsigned long long **counter, float **rec,
                           PointMeta **meta, int2 **rows, double **part, double **band,
-                          double **obs_vx) {
+                          double **obs_vx, GeoShared **setup) {
     *counter = c.take<unsigned long long>(4);
+    *setup = c.take<GeoShared>((size_t)L.setup_pts);
     *rec = c.take<float>((size_t)L.batch * L.rec_words);
     *meta = c.take<PointMeta>((size_t)L.batch);
     *rows = c.take<int2>((size_t)L.batch * WAKE_MAX_REGIONS);
@@ -919,7 +960,8 @@ extern "C" size_t dfcsr_wake_workspace_bytes(int xbins_max, int zbins_max, int64
     PointMeta *m;
     int2 *rw;
     double *p, *q, *v;
-    return mixed_carve(c, L, &a, &b, &m, &rw, &p, &q, &v) + 256;
+    GeoShared *g;
+    return mixed_carve(c, L, &a, &b, &m, &rw, &p, &q, &v, &g) + 256;
 }
 
 extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
@@ -941,7 +983,8 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
     PointMeta *meta;
     int2 *rows;
     double *part, *band, *obs_vx;
-    mixed_carve(c, L, &counter, &rec, &meta, &rows, &part, &band, &obs_vx);
+    GeoShared *setup;
+    mixed_carve(c, L, &counter, &rec, &meta, &rows, &part, &band, &obs_vx, &setup);
     if (!workspace || !c.ok()) {
         set_error("dfcsr_wake_mixed: workspace too small (%zu < %zu)", workspace_bytes, c.used);
         return DFCSR_OOM;
@@ -956,13 +999,21 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
     const int max_rows = 2 * xbins_max;
     const size_t smem = integral_smem_bytes(max_rows);
     const int blocks_max = integral_blocks(smem);
+    int64_t setup_first = 0, setup_count = 0;
     for (int64_t first = 0; first < n; first += L.batch) {
         const int64_t count = (n - first < L.batch) ? n - first : L.batch;
         DFCSR_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
         {
             ScopedTiming tm("wake_mixed_geometry", st);
+            if (first + count > setup_first + setup_count) {   // next set-up chunk
+                setup_first = first;
+                setup_count = (n - first < L.setup_pts) ? n - first : L.setup_pts;
+                mixed_setup<<<(unsigned)setup_count, SETUP_THREADS, 0, st>>>(
+                    jobs, job_of_point, s, x, setup_first, setup_count, L.rec_words, max_rows, setup);
+            }
             mixed_geometry<<<(unsigned)count, GEO_THREADS, 0, st>>>(
-                jobs, job_of_point, s, x, first, count, L.rec_words, max_rows, rec, meta, rows, obs_vx);
+                jobs, job_of_point, s, x, first, count, setup + (first - setup_first), L.rec_words, rec,
+                meta, rows, obs_vx);
         }
         const int blocks = (int)((int64_t)blocks_max < count ? blocks_max : count);
         {
