@@ -113,6 +113,42 @@ __device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *
     if ((size_t)off > rec_words) ok = false;
 }
 
+// interpolate3D of one history field from the axis coordinates
+// u = (t - t_min) / t_delta, ... (computed by the caller), FP64.
+__device__ inline double hist_field_u(const dfcsr_wake_job &J, int field, double ut, double ux, double uz) {
+    int t0, t1, x0, x1, z0, z1;
+    double td, xd, zd;
+    if (!axis_index(ut, J.nt, t0, t1, td) || !axis_index(ux, J.nx, x0, x1, xd) ||
+        !axis_index(uz, J.nz, z0, z1, zd))
+        return 0.0;
+    const int s0 = ring_slot(J, t0), s1 = ring_slot(J, t1);
+    auto D = [&](int s, int xi, int zi) -> double {
+        const size_t cell = ((size_t)s * J.nx + xi) * J.nz + zi;
+        return J.ring64 ? J.ring64[cell * 5 + field] : (double)J.ring32[cell * 8 + field];
+    };
+    const double c00 = D(s0, x0, z0) * (1 - td) + D(s1, x0, z0) * td;
+    const double c01 = D(s0, x0, z1) * (1 - td) + D(s1, x0, z1) * td;
+    const double c10 = D(s0, x1, z0) * (1 - td) + D(s1, x1, z0) * td;
+    const double c11 = D(s0, x1, z1) * (1 - td) + D(s1, x1, z1) * td;
+    const double c0 = c00 * (1 - xd) + c10 * xd;
+    const double c1 = c01 * (1 - xd) + c11 * xd;
+    return c0 * (1 - zd) + c1 * zd;
+}
+
+// The six orbit tables from the table coordinate u = (s - s_min) / s_delta.
+__device__ __forceinline__ void lattice_lerp_u(const dfcsr_wake_job &J, double u, double out[6]) {
+    int a, b;
+    double f;
+    if (!axis_index(u, J.nsample, a, b, f)) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) out[k] = 0.0;
+        return;
+    }
+    const double *pa = J.lattice + (size_t)a * 6, *pb = J.lattice + (size_t)b * 6;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) out[k] = pa[k] * (1 - f) + pb[k] * f;
+}
+
 struct alignas(16) GeoShared {
     Region reg[WAKE_MAX_REGIONS];
     RegionMeta rm[WAKE_MAX_REGIONS];
@@ -141,6 +177,7 @@ struct alignas(16) GeoShared {
     float rhof[WAKE_MAX_REGIONS][GEO_MAXB + 1];
     float band_f;
     float inv_dt_f, inv_dz_f;   // FP32 reciprocals of the history t and z steps
+    double inv_s, inv_x;        // reciprocals of the orbit-table and history x steps
 };
 
 __device__ __forceinline__ int cell_of(float fl, bool nan) {
@@ -374,12 +411,31 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
     const double t = J.position, s = S[pt], x = X[pt];
     const bool use_dw = J.lattice_dw != nullptr && J.lattice_delta_dw != nullptr;
     // the independent per-point set-up tasks run in separate warps
-    if (threadIdx.x == 32) {
-        gs.vx_obs = hist_field_fp64(J, 3, t, x, s - t);
-        gs.vxw = dw_from(gs.vx_obs);
-    } else if (threadIdx.x == 33) {
-        lattice_lerp(J, s, gs.lat_s);
-        if (use_dw) {
+    if (threadIdx.x >= 32) {
+        // warp 1: the eight quotients of the set-up in ONE warp-wide FP64
+        // division (lane l), instead of eight divisions issued one after
+        // another by single threads (an FP64 instruction costs the SM's FP64
+        // unit the same time for one active lane as for 32)
+        const int l = threadIdx.x - 32;
+        double num = 1.0, den = 1.0;
+        if (l == 0) { num = t - J.t_min; den = J.t_delta; }
+        else if (l == 1) { num = x - J.x_min; den = J.x_delta; }
+        else if (l == 2) { num = (s - t) - J.z_min; den = J.z_delta; }
+        else if (l == 3) { num = s - J.s_min; den = J.s_delta; }
+        else if (l == 4) den = J.t_delta;
+        else if (l == 5) den = J.z_delta;
+        else if (l == 6) den = J.s_delta;
+        else if (l == 7) den = J.x_delta;
+        const double q = num / den;
+        double qv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) qv[k] = __shfl_sync(0xffffffffu, q, k);
+        if (l == 0) {
+            gs.vx_obs = hist_field_u(J, 3, qv[0], qv[1], qv[2]);
+            gs.vxw = dw_from(gs.vx_obs);
+        } else if (l == 1) {
+            lattice_lerp_u(J, qv[3], gs.lat_s);
+            if (use_dw) {
             const double nx_ = gs.lat_s[2], ny_ = gs.lat_s[3];
             gs.Px = dw_from(fma(x, nx_, gs.lat_s[0]));
             gs.Py = dw_from(fma(x, ny_, gs.lat_s[1]));
@@ -388,16 +444,21 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
             gs.tsx = dw_from(gs.lat_s[4]);
             gs.tsy = dw_from(gs.lat_s[5]);
         }
-    } else if (threadIdx.x == 34) {
-        if (use_dw) {
-            gs.T0 = dw_from(t - J.t_min);
-            gs.Tz = dw_from(t + J.z_min);
-            gs.inv_t = dw_from(1.0 / J.t_delta);
-            gs.inv_z = dw_from(1.0 / J.z_delta);
-            gs.Sw = dw_from(s);
-            gs.band_f = J.near_band > 0.0 ? (float)J.near_band : 0.f;
+        } else if (l == 2) {
+            gs.inv_dt_f = (float)qv[4];
+            gs.inv_dz_f = (float)qv[5];
+            gs.inv_s = qv[6];
+            gs.inv_x = qv[7];
+            if (use_dw) {
+                gs.T0 = dw_from(t - J.t_min);
+                gs.Tz = dw_from(t + J.z_min);
+                gs.inv_t = dw_from(qv[4]);
+                gs.inv_z = dw_from(qv[5]);
+                gs.Sw = dw_from(s);
+                gs.band_f = J.near_band > 0.0 ? (float)J.near_band : 0.f;
+            }
         }
-    } else if (threadIdx.x < 32) {
+    } else {
         // warp 0: lane 0 finds the regions and the record layout, then one
         // lane per region sets up that region's axes and element thresholds
         if (threadIdx.x == 0) {
@@ -408,8 +469,6 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
             // that is not 32-byte aligned makes the point invalid (NaN result)
             if (((uintptr_t)J.ring32 & 31u) != 0) ok = false;
             gs.ok = ok ? 1 : 0;
-            gs.inv_dt_f = (float)(1.0 / J.t_delta);
-            gs.inv_dz_f = (float)(1.0 / J.z_delta);
             int cb = 0, rb = 0;
             for (int r = 0; r < gs.nreg; ++r) {
                 gs.col_begin[r] = cb;
@@ -457,18 +516,24 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
             gs.wxf[r][0] = AX.n < 2 ? 0.f : (float)(0.5 * AX.step);
             gs.wxf[r][1] = AX.n < 2 ? 0.f : (float)AX.step;
             if (use_dw) {
-                const double inv_s = 1.0 / J.s_delta, inv_x = 1.0 / J.x_delta;
                 gs.S0[r] = dw_from(A.start);
                 gs.Sst[r] = dw_from(A.step);
-                gs.U0[r] = dw_from((A.start - J.s_min) * inv_s);
-                gs.Ust[r] = dw_from(A.step * inv_s);
                 gs.X0[r] = dw_from(AX.start);
                 gs.Xst[r] = dw_from(AX.step);
-                gs.UX0[r] = dw_from((AX.start - J.x_min) * inv_x);
-                gs.UXst[r] = dw_from(AX.step * inv_x);
                 gs.xrefw[r] = dw_from(gs.xref[r]);
             }
         }
+    }
+    __syncthreads();
+    // orbit-table and history coordinates of the axes (need warp 1's
+    // reciprocals)
+    if (use_dw && threadIdx.x < gs.nreg) {
+        const int r = threadIdx.x;
+        const Axis A = gs.ax_s[r], AX = gs.ax_x[r];
+        gs.U0[r] = dw_from((A.start - J.s_min) * gs.inv_s);
+        gs.Ust[r] = dw_from(A.step * gs.inv_s);
+        gs.UX0[r] = dw_from((AX.start - J.x_min) * gs.inv_x);
+        gs.UXst[r] = dw_from(AX.step * gs.inv_x);
     }
     __syncthreads();
     // the finished record to global memory
