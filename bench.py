@@ -407,12 +407,12 @@ def gpu_arm(a):
                                           "launch; gathers are served mostly from L1/L2",
                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
         if a.precision == "mixed":
-            # DRAM bytes and FP32 operations per integrand point from the ncu
-            # capture in profiles/wake_mixed_integral_chicane_2e6.md (42.2 MB
-            # and 2.20 GFLOP for a launch of 4.01e7 integrand points), scaled
-            # to this launch size
-            traffic = 42.2e6 / 4.01e7 * per_launch_pts
-            flops = 2.20e9 / 4.01e7 * per_launch_pts
+            # DRAM bytes and FP32 operations per integrand point from an ncu
+            # capture of this kernel on this workload (89.4 MB and 4.79 GFLOP
+            # for a launch of 8.275e7 integrand points), scaled to this
+            # launch size
+            traffic = 89.36e6 / 8.275e7 * per_launch_pts
+            flops = 4.79e9 / 8.275e7 * per_launch_pts
             fp32_peak = fma_peaks["fp32_tflops"]
             out["roofline"]["traffic"] = traffic
             out["roofline"]["dram_frac"] = traffic / (launch_ms * 1e-3) / 1e9 / hbm
@@ -420,9 +420,10 @@ def gpu_arm(a):
                 "achieved_tflops": flops / (launch_ms * 1e-3) / 1e12, "peak_tflops": fp32_peak,
                 "frac": flops / (launch_ms * 1e-3) / 1e12 / fp32_peak,
                 "peak_source": "measured FMA rate (peaks_measured)"}
-            out["roofline"]["binding"] = ("gather latency / L1TEX: eight 32-byte history cells per "
-                                          "integrand point from L1/L2 (L1TEX 68 % of peak, top stall "
-                                          "long_scoreboard, issue 49 % in ncu)")
+            out["roofline"]["binding"] = ("gathers / L1TEX: eight 32-byte history cells per integrand "
+                                          "point from L1/L2 (L1TEX 74 % of peak: data-pipe wavefronts "
+                                          "72 %, LSU writeback 65 %; top stall long_scoreboard, issue "
+                                          "56 % in ncu)")
     out["peaks_measured"] = fma_peaks
     out["gpu_launches"] = int(sum(launches.values()))
     out["kernel_launches_by_name"] = launches
