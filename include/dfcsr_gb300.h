@@ -140,7 +140,9 @@ typedef struct {
 
 /* density, vx: in = raw deposits, out = final fields.  density_x,
  * density_z, vx_x: outputs.  scalars_out[8] (device): 0 dsum, 1 thr,
- * 2 thr2, 3 vx_x fill, 4 mean(vx_x), 5 max raw density, 6 max density.
+ * 2 thr2, 3 vx_x fill, 4 mean(vx_x), 5 max raw density, 6 max density
+ * (all NaN if a grid barrier of the launch timed out).  nz <= 16384.
+ * One cooperative launch (one CTA per SM, all resident) on `stream`.
  * Scratch: dfcsr_df_workspace_bytes(nx, nz). */
 size_t dfcsr_df_workspace_bytes(int nx, int nz);
 int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, double *vx,
