@@ -212,15 +212,29 @@ radix_scan_rows(uint32_t *__restrict__ hist, int ntiles, uint32_t *__restrict__ 
     if (threadIdx.x == 0) dtot[blockIdx.x] = carry_s;
 }
 
+// Stable scatter of one tile (RS_TILE keys): warp-level ranks of equal
+// digits (__match_any_sync, in element order), then the tile is reordered by
+// digit in shared memory and written out so that consecutive threads write
+// consecutive positions of a digit's run (coalesced stores instead of one
+// scattered 4-byte store per key).
+struct ScatterSmem {
+    union {
+        uint32_t wcnt[RS_WARPS][RS_BINS];             // ranking phase
+        struct { uint32_t key[RS_TILE], val[RS_TILE]; } t;   // reordered tile
+    } u;
+    uint32_t dbase[RS_BINS];   // global start of each digit
+    uint32_t toff[RS_BINS];    // tile-local start of each digit
+};
+
 __global__ void __launch_bounds__(RS_THREADS)
 radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, int64_t n,
               int shift, int ntiles, const uint32_t *__restrict__ hist,
               const uint32_t *__restrict__ dtot, uint32_t *__restrict__ keys_out,
               uint32_t *__restrict__ vals_out) {
-    __shared__ uint32_t wcnt[RS_WARPS][RS_BINS];
-    __shared__ uint32_t dbase[RS_BINS];
+    extern __shared__ __align__(16) unsigned char rs_smem[];
+    ScatterSmem &sm = *reinterpret_cast<ScatterSmem *>(rs_smem);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int d = threadIdx.x; d < RS_WARPS * RS_BINS; d += RS_THREADS) (&wcnt[0][0])[d] = 0;
+    for (int d = threadIdx.x; d < RS_WARPS * RS_BINS; d += RS_THREADS) (&sm.u.wcnt[0][0])[d] = 0;
     if (warp == 0) {
         // exclusive scan of the digit totals (RS_BINS / 32 per lane)
         constexpr int PER = RS_BINS / 32;
@@ -232,10 +246,11 @@ radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ va
             if (lane >= o) inc += t;
         }
         uint32_t run = inc - s;
-        for (int k = 0; k < PER; ++k) { dbase[lane * PER + k] = run; run += loc[k]; }
+        for (int k = 0; k < PER; ++k) { sm.dbase[lane * PER + k] = run + hist[(size_t)(lane * PER + k) * ntiles + blockIdx.x]; run += loc[k]; }
     }
     __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)warp * (32 * RS_ITEMS);
+    const int64_t tile0 = (int64_t)blockIdx.x * RS_TILE;
+    const int64_t base = tile0 + (int64_t)warp * (32 * RS_ITEMS);
     uint32_t k[RS_ITEMS], v[RS_ITEMS], rank[RS_ITEMS];
     int dig[RS_ITEMS];
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -248,9 +263,9 @@ radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ va
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const int leader = __ffs(peers) - 1;
         uint32_t before = 0;
-        if (valid) before = wcnt[warp][d];
+        if (valid) before = sm.u.wcnt[warp][d];
         __syncwarp();
-        if (valid && lane == leader) wcnt[warp][d] = before + __popc(peers);
+        if (valid && lane == leader) sm.u.wcnt[warp][d] = before + __popc(peers);
         __syncwarp();
         rank[r] = before + __popc(peers & lt_mask);
         dig[r] = d;
@@ -258,23 +273,50 @@ radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ va
         v[r] = valid ? vals[idx] : 0u;
     }
     __syncthreads();
+    // per digit: exclusive prefix over the warps (in place) and the tile total
     for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) {
         uint32_t run = 0;
         for (int w = 0; w < RS_WARPS; ++w) {
-            const uint32_t t = wcnt[w][d];
-            wcnt[w][d] = run;
+            const uint32_t t = sm.u.wcnt[w][d];
+            sm.u.wcnt[w][d] = run;
             run += t;
+        }
+        sm.toff[d] = run;
+    }
+    __syncthreads();
+    if (warp == 0) {   // tile-local digit starts: exclusive scan of the totals
+        constexpr int PER = RS_BINS / 32;
+        uint32_t loc[PER], s = 0;
+        for (int q = 0; q < PER; ++q) { loc[q] = sm.toff[lane * PER + q]; s += loc[q]; }
+        uint32_t inc = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        uint32_t run = inc - s;
+        for (int q = 0; q < PER; ++q) { sm.toff[lane * PER + q] = run; run += loc[q]; }
+    }
+    __syncthreads();
+    // rank -> tile-local position
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; ++r)
+        if (dig[r] < RS_BINS) rank[r] += sm.toff[dig[r]] + sm.u.wcnt[warp][dig[r]];
+    __syncthreads();   // wcnt is overwritten by the reordered tile
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        if (dig[r] < RS_BINS) {
+            sm.u.t.key[rank[r]] = k[r];
+            sm.u.t.val[rank[r]] = v[r];
         }
     }
     __syncthreads();
-#pragma unroll
-    for (int r = 0; r < RS_ITEMS; ++r) {
-        const int d = dig[r];
-        if (d < RS_BINS) {
-            const uint32_t pos = dbase[d] + hist[(size_t)d * ntiles + blockIdx.x] + wcnt[warp][d] + rank[r];
-            keys_out[pos] = k[r];
-            vals_out[pos] = v[r];
-        }
+    const int cnt = (int)((n - tile0) < RS_TILE ? (n - tile0) : RS_TILE);
+    for (int i = threadIdx.x; i < cnt; i += RS_THREADS) {
+        const uint32_t key = sm.u.t.key[i];
+        const int d = (int)((key >> shift) & RS_MASK);
+        const uint32_t pos = sm.dbase[d] + (uint32_t)i - sm.toff[d];
+        keys_out[pos] = key;
+        vals_out[pos] = sm.u.t.val[i];
     }
 }
 
@@ -595,8 +637,8 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
             const int shift = RS_BITS * p;
             radix_upsweep<<<L.ntiles, RS_THREADS, 0, s>>>(kin, n, shift, L.ntiles, hist);
             radix_scan_rows<<<RS_BINS, 1024, 0, s>>>(hist, L.ntiles, dtot);
-            radix_scatter<<<L.ntiles, RS_THREADS, 0, s>>>(kin, vin, n, shift, L.ntiles, hist, dtot,
-                                                          kout, vout);
+            radix_scatter<<<L.ntiles, RS_THREADS, sizeof(ScatterSmem), s>>>(kin, vin, n, shift, L.ntiles,
+                                                                             hist, dtot, kout, vout);
             uint32_t *t = kin; kin = kout; kout = t;
             t = vin; vin = vout; vout = t;
         }
