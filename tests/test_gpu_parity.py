@@ -156,6 +156,29 @@ def _device_run_from_fixture(g, precision="both"):
 
 
 @cuda
+@pytest.mark.parametrize("nx,nz,win,order", [(33, 47, 5, 2), (259, 31, 9, 1), (200, 130, 21, 3),
+                                             (70, 300, 63, 2), (600, 40, 11, 2)])
+def test_df_stage_shapes_vs_oracle(nx, nz, win, order):
+    """The one-launch DF finalisation on grids that are not multiples of its
+    32 x 32 smoothing tiles or 32-row trapz chunks, z lengths above one CTA,
+    the longest window, against the oracle on the same particles: 1e-10 of
+    each field's maximum (sums are evaluated in fixed orders of their own)."""
+    from pydfcsr_gb300.deposit import DF_tracker
+    from pydfcsr_gb300.synthetic import gaussian_beam
+    b = gaussian_beam(40000, 10e-6, 20e-6, 1e-4, 5e-6, -8.0, seed=nx * 1000 + nz)
+    dep = {"xbins": nx, "zbins": nz, "xlim": 5, "zlim": 5, "filter_order": order,
+           "filter_window": win, "velocity_threhold": 1000}
+    dev = DF_tracker(dep, grid_rule="configured")
+    orc = O.DFTracker(dep, grid_rule="configured")
+    dev.get_DF(b[0], b[4], b[1], 0.25)
+    orc.get_DF(b[0], b[4], b[1], 0.25)
+    for k in ("density", "vx", "density_x", "density_z", "vx_x"):
+        out, ref = getattr(dev, k), getattr(orc, k)
+        assert out.shape == ref.shape == (nx, nz), k
+        assert _maxrel(out, ref) < 1e-10, (k, _maxrel(out, ref))
+
+
+@cuda
 @pytest.mark.parametrize("tag", ["dipole", "chicane_pos", "chicane_neg", "dipole_big"])
 def test_wake_fp64_golden(tag):
     g = golden(f"wake_{tag}.npz")
