@@ -2,27 +2,32 @@
 //
 // Same integral as get_CSR_wake / get_CSR_integrand (pyDFCSR_2D/CSR.py:454-782),
 // restructured so that FP32 is safe and little work is wasted:
+//  * set-up kernel (FP64), one small CTA per observation point: regions,
+//    record layout, orbit at s, vx at the observer, axes, element
+//    thresholds and the double-word per-point constants, written as one
+//    record per point.
 //  * geometry kernel (double-word FP32 from the job's double-word orbit
 //    tables, ~48 bits; FP64 for jobs without them), one CTA per observation
 //    point: per s' column the orbit tables at s', the separation R0 = r - r'
-//    at a reference x' (the region centre), |R0|, the history coordinates of t_ret and
-//    s' - t_ret, and every direction product whose difference would cancel in
-//    FP32 (v.tau', v.n', 1 - |tau'|^2, |n'|^2 - 1, (r - r').(n - n'), ...);
-//    per x' row the history x cell and the trapz weight, and the range of rows
-//    whose x' lies inside the history grid (outside it every field, hence the
-//    integrand, is exactly zero, so those rows are skipped).  Records are
-//    written for a batch of points small enough to stay resident in L2.
+//    at a reference x' (the region centre), |R0|, the history coordinates of
+//    t_ret and s' - t_ret, and every direction product whose difference would
+//    cancel in FP32 (v.tau', v.n', 1 - |tau'|^2, |n'|^2 - 1,
+//    (r - r').(n - n'), ...); per x' row the history x cell and the trapz
+//    weight, and the range of rows whose x' lies inside the history grid
+//    (outside it every field, hence the integrand, is exactly zero, so those
+//    rows are skipped).  Records are written for a batch of points small
+//    enough to stay resident in L2.
 //  * integral kernel (FP32), a persistent CTA loop over points: per (x', s')
 //    only an FP32 correction remains,
 //        |r - r'| = r0 + delta,  delta = D / (r0 + sqrt(r0^2 + D)),
 //        D = u (|n'|^2 u - 2 R0.n'),  u = x' - x'_ref   (no cancellation);
-//    history coordinates are an integer cell (from FP64) plus an FP32
-//    offset, so a grid index near 1000 keeps ~1e-7 cell resolution; the x'
-//    axis (index and weight) is resolved once per row in FP64; gathers and
-//    the integrand are FP32 (in the far region density_x, whose x' integral
-//    cancels, is read as a stored hi + lo pair and interpolated in offset
-//    form so that it is rounded once), Kahan-compensated per-thread sums and
-//    a fixed-order FP64 block reduction.
+//    history coordinates are an integer cell plus an FP32 offset, so a grid
+//    index near 1000 keeps ~1e-7 cell resolution; the x' axis (index and
+//    weight) is resolved once per row; gathers and the integrand are FP32
+//    (in the far region density_x, whose x' integral cancels, is read as a
+//    stored hi + lo pair and interpolated in offset form so that it is
+//    rounded once), Kahan-compensated per-thread sums and a fixed-order
+//    block reduction in FP32 double-word.
 //  * band kernel (FP64, optional): s' columns with |s' - s| < near_band are
 //    skipped by the integral kernel and evaluated with the FP64 integrand.
 //  * finalize kernel: adds the regions in the reference's order and scales.
