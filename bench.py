@@ -115,8 +115,37 @@ def lattice_for(wl, total_steps):
 
 
 # ------------------------------------------------------------------ clocks
+# NVML poller run as a subprocess (no GIL contention with the step loop):
+# one line "wall time, SM MHz, max SM MHz, event-reason bits" every 2 ms.
+_NVML_POLLER = r"""
+import ctypes, sys, time
+lib = ctypes.CDLL("libnvidia-ml.so.1")
+if lib.nvmlInit_v2() != 0:
+    sys.exit(1)
+h = ctypes.c_void_p()
+if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(int(sys.argv[1])), ctypes.byref(h)) != 0:
+    sys.exit(1)
+clk, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))          # NVML_CLOCK_SM
+reasons = (getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+           or lib.nvmlDeviceGetCurrentClocksThrottleReasons)
+while True:
+    lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk))
+    reasons(h, ctypes.byref(rs))
+    sys.stdout.write("%.6f,%d,%d,%d\n" % (time.time(), clk.value, mx.value, rs.value))
+    sys.stdout.flush()
+    time.sleep(0.002)
+"""
+
+# NVML clock event reason bits (nvml.h) reported by the benchmark
+_REASON_BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+                0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+
 class ClockSampler:
-    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    """SM clocks and throttle reasons during a region: NVML polled every 2 ms
+    by a subprocess (samples inside [mark_start, mark_end] are kept), else
+    nvidia-smi every 200 ms."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -126,17 +155,40 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.nvml = False
+        self.t0 = self.t1 = None
+
+    def _spawn(self, argv):
+        self.proc = subprocess.Popen(argv, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                     text=True)
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
 
     def start(self):
+        """Start sampling; with NVML, wait (at most 10 s) for the first sample."""
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
-        except (OSError, FileNotFoundError):
+            self._spawn([sys.executable, "-c", _NVML_POLLER, str(self.index)])
+            t_end = time.time() + 10.0
+            while not self.lines and self.proc.poll() is None and time.time() < t_end:
+                time.sleep(0.005)
+            if self.lines:
+                self.nvml = True
+                return
+            self.proc.kill()
+        except OSError:
+            pass
+        self.lines = []
+        try:
+            self._spawn(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                         "--format=csv,noheader,nounits", "-lms", "200"])
+        except OSError:
             self.proc = None
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
 
     def _read(self):
         for line in self.proc.stdout:
@@ -151,6 +203,23 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         sm, mx, reasons = [], [], set()
+        if self.nvml:
+            for ln in list(self.lines):
+                f = ln.split(",")
+                if len(f) != 4:
+                    continue
+                ts, clk, mxc, bits = float(f[0]), float(f[1]), float(f[2]), int(f[3])
+                if self.t0 is not None and not (self.t0 <= ts <= (self.t1 or ts)):
+                    continue
+                sm.append(clk)
+                mx.append(mxc)
+                for bit, nm in _REASON_BITS.items():
+                    if bits & bit:
+                        reasons.add(nm)
+            return {"sm_mhz": float(np.median(sm)) if sm else None,
+                    "sm_max_mhz": float(max(mx)) if mx else None,
+                    "reasons": sorted(reasons), "samples": len(sm),
+                    "source": "NVML, every 2 ms, inside the timed region"}
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
@@ -166,7 +235,8 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": float(max(mx)) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "source": "nvidia-smi, every 200 ms"}
 
 
 # -------------------------------------------------------------- GPU arm
@@ -351,10 +421,12 @@ def gpu_arm(a):
     barrier()
     t0 = time.perf_counter()
     step_events = []
+    clocks.mark_start()
     e0.record(stream)
     timed_steps(run, sets, W + 1, K, a.precision, events=step_events, side=side)
     e1.record(stream)
     barrier()
+    clocks.mark_end()
     wall = time.perf_counter() - t0
     ck = clocks.stop()
     _lib.timing_enable(False)
