@@ -480,11 +480,11 @@ def gpu_arm(a):
                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
         if a.precision == "mixed":
             # DRAM bytes and FP32 operations per integrand point from an ncu
-            # capture of this kernel on this workload (89.4 MB and 4.79 GFLOP
-            # for a launch of 8.275e7 integrand points), scaled to this
+            # capture of this kernel on this workload (204.4 MB and 11.9
+            # GFLOP for a launch of 2.048e8 integrand points), scaled to this
             # launch size
-            traffic = 89.36e6 / 8.275e7 * per_launch_pts
-            flops = 4.79e9 / 8.275e7 * per_launch_pts
+            traffic = 204.4e6 / 2.048e8 * per_launch_pts
+            flops = 1.19e10 / 2.048e8 * per_launch_pts
             fp32_peak = fma_peaks["fp32_tflops"]
             out["roofline"]["traffic"] = traffic
             out["roofline"]["dram_frac"] = traffic / (launch_ms * 1e-3) / 1e9 / hbm
@@ -493,9 +493,9 @@ def gpu_arm(a):
                 "frac": flops / (launch_ms * 1e-3) / 1e12 / fp32_peak,
                 "peak_source": "measured FMA rate (peaks_measured)"}
             out["roofline"]["binding"] = ("gathers / L1TEX: eight 32-byte history cells per integrand "
-                                          "point from L1/L2 (L1TEX 74 % of peak: data-pipe wavefronts "
-                                          "72 %, LSU writeback 65 %; top stall long_scoreboard, issue "
-                                          "56 % in ncu)")
+                                          "point from L1/L2 (L1TEX 77 % of peak: data-pipe wavefronts "
+                                          "76 %, LSU writeback 68 %; top stall long_scoreboard, issue "
+                                          "59 % in ncu)")
     out["peaks_measured"] = fma_peaks
     out["gpu_launches"] = int(sum(launches.values()))
     out["kernel_launches_by_name"] = launches

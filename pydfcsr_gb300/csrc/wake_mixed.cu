@@ -15,8 +15,8 @@
 //    (r - r').(n - n'), ...); per x' row the history x cell and the trapz
 //    weight, and the range of rows whose x' lies inside the history grid
 //    (outside it every field, hence the integrand, is exactly zero, so those
-//    rows are skipped).  Records are written for a batch of points small
-//    enough to stay resident in L2.
+//    rows are skipped).  Records are written for a batch of points (up to
+//    1 GiB of records: one batch for a 64^2 mesh).
 //  * integral kernel (FP32), a persistent CTA loop over points: per (x', s')
 //    only an FP32 correction remains,
 //        |r - r'| = r0 + delta,  delta = D / (r0 + sqrt(r0^2 + D)),
