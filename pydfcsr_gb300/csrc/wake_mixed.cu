@@ -118,40 +118,10 @@ __device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *
     if ((size_t)off > rec_words) ok = false;
 }
 
-// interpolate3D of one history field from the axis coordinates
-// u = (t - t_min) / t_delta, ... (computed by the caller), FP64.
-__device__ inline double hist_field_u(const dfcsr_wake_job &J, int field, double ut, double ux, double uz) {
-    int t0, t1, x0, x1, z0, z1;
-    double td, xd, zd;
-    if (!axis_index(ut, J.nt, t0, t1, td) || !axis_index(ux, J.nx, x0, x1, xd) ||
-        !axis_index(uz, J.nz, z0, z1, zd))
-        return 0.0;
-    const int s0 = ring_slot(J, t0), s1 = ring_slot(J, t1);
-    auto D = [&](int s, int xi, int zi) -> double {
-        const size_t cell = ((size_t)s * J.nx + xi) * J.nz + zi;
-        return J.ring64 ? J.ring64[cell * 5 + field] : (double)J.ring32[cell * 8 + field];
-    };
-    const double c00 = D(s0, x0, z0) * (1 - td) + D(s1, x0, z0) * td;
-    const double c01 = D(s0, x0, z1) * (1 - td) + D(s1, x0, z1) * td;
-    const double c10 = D(s0, x1, z0) * (1 - td) + D(s1, x1, z0) * td;
-    const double c11 = D(s0, x1, z1) * (1 - td) + D(s1, x1, z1) * td;
-    const double c0 = c00 * (1 - xd) + c10 * xd;
-    const double c1 = c01 * (1 - xd) + c11 * xd;
-    return c0 * (1 - zd) + c1 * zd;
-}
-
-// The six orbit tables from the table coordinate u = (s - s_min) / s_delta.
-__device__ __forceinline__ void lattice_lerp_u(const dfcsr_wake_job &J, double u, double out[6]) {
-    int a, b;
-    double f;
-    if (!axis_index(u, J.nsample, a, b, f)) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) out[k] = 0.0;
-        return;
-    }
-    const double *pa = J.lattice + (size_t)a * 6, *pb = J.lattice + (size_t)b * 6;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) out[k] = pa[k] * (1 - f) + pb[k] * f;
+// One history field at (slot, x, z) from the FP64 ring, else the FP32 ring.
+__device__ __forceinline__ double hist_cell(const dfcsr_wake_job &J, int field, int slot, int xi, int zi) {
+    const size_t cell = ((size_t)slot * J.nx + xi) * J.nz + zi;
+    return J.ring64 ? J.ring64[cell * 5 + field] : (double)J.ring32[cell * 8 + field];
 }
 
 struct alignas(16) GeoShared {
@@ -435,33 +405,92 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
         double qv[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) qv[k] = __shfl_sync(0xffffffffu, q, k);
-        if (l == 0) {
-            gs.vx_obs = hist_field_u(J, 3, qv[0], qv[1], qv[2]);
-            gs.vxw = dw_from(gs.vx_obs);
-        } else if (l == 1) {
-            lattice_lerp_u(J, qv[3], gs.lat_s);
-            if (use_dw) {
-            const double nx_ = gs.lat_s[2], ny_ = gs.lat_s[3];
-            gs.Px = dw_from(fma(x, nx_, gs.lat_s[0]));
-            gs.Py = dw_from(fma(x, ny_, gs.lat_s[1]));
-            gs.nsx = dw_from(nx_);
-            gs.nsy = dw_from(ny_);
-            gs.tsx = dw_from(gs.lat_s[4]);
-            gs.tsy = dw_from(gs.lat_s[5]);
+        // axis indices in one pass: lanes 0..2 the history t, x, z of vx at
+        // the observer, lane 3 the orbit-table index of s
+        const double uu = q;   // lanes 0..3 hold these quotients themselves
+        const int nn = (l == 0) ? J.nt : (l == 1) ? J.nx : (l == 2) ? J.nz : J.nsample;
+        int i0 = 0, i1 = 0;
+        double fr = 0.0;
+        const bool in = l < 4 && axis_index(uu, nn, i0, i1, fr);
+        const unsigned inm = __ballot_sync(0xffffffffu, in);
+        const bool hist_in = (inm & 7u) == 7u, lat_in = (inm & 8u) != 0u;
+        const int t0 = __shfl_sync(0xffffffffu, i0, 0), t1 = __shfl_sync(0xffffffffu, i1, 0);
+        const int x0 = __shfl_sync(0xffffffffu, i0, 1), x1 = __shfl_sync(0xffffffffu, i1, 1);
+        const int z0 = __shfl_sync(0xffffffffu, i0, 2), z1 = __shfl_sync(0xffffffffu, i1, 2);
+        const int a0 = __shfl_sync(0xffffffffu, i0, 3), a1 = __shfl_sync(0xffffffffu, i1, 3);
+        const double td = __shfl_sync(0xffffffffu, fr, 0), xd = __shfl_sync(0xffffffffu, fr, 1);
+        const double zd = __shfl_sync(0xffffffffu, fr, 2), lf = __shfl_sync(0xffffffffu, fr, 3);
+        // one warp-wide lerp: lanes 0..3 the t-lerps of vx at the four (x, z)
+        // history corners (lane = 2 xi + zi), lanes 4..9 the six orbit tables
+        // at s (interpolate3D / interpolate1D arithmetic)
+        double pa = 0.0, pb = 0.0, wgt = 0.0;
+        if (l < 4) {
+            if (hist_in) {
+                const int xi = (l & 2) ? x1 : x0, zi = (l & 1) ? z1 : z0;
+                const int s0 = ring_slot(J, t0), s1 = ring_slot(J, t1);
+                pa = hist_cell(J, 3, s0, xi, zi);
+                pb = hist_cell(J, 3, s1, xi, zi);
+                wgt = td;
+            }
+        } else if (l < 10) {
+            if (lat_in) {
+                pa = J.lattice[(size_t)a0 * 6 + (l - 4)];
+                pb = J.lattice[(size_t)a1 * 6 + (l - 4)];
+                wgt = lf;
+            }
         }
-        } else if (l == 2) {
+        const double lv = pa * (1 - wgt) + pb * wgt;
+        // then x (lanes 0, 1: z0 and z1) and z
+        const double cx1 = __shfl_sync(0xffffffffu, lv, (l & 1) + 2);
+        const double e = lv * (1 - xd) + cx1 * xd;
+        const double e1 = __shfl_sync(0xffffffffu, e, 1);
+        const double vx_obs = __shfl_sync(0xffffffffu, hist_in ? e * (1 - zd) + e1 * zd : 0.0, 0);
+        double lat[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) lat[k] = lat_in ? __shfl_sync(0xffffffffu, lv, 4 + k) : 0.0;
+        if (l == 0) gs.vx_obs = vx_obs;
+        if (l >= 4 && l < 10) gs.lat_s[l - 4] = lat_in ? lv : 0.0;
+        // the per-point double-word constants in one warp-wide conversion
+        double dv = 0.0;
+        switch (l) {
+            case 0: dv = fma(x, lat[2], lat[0]); break;   // r(s) + x n(s)
+            case 1: dv = fma(x, lat[3], lat[1]); break;
+            case 2: dv = lat[2]; break;
+            case 3: dv = lat[3]; break;
+            case 4: dv = lat[4]; break;
+            case 5: dv = lat[5]; break;
+            case 6: dv = t - J.t_min; break;
+            case 7: dv = t + J.z_min; break;
+            case 8: dv = qv[4]; break;
+            case 9: dv = qv[5]; break;
+            case 10: dv = s; break;
+            case 11: dv = vx_obs; break;
+            default: break;
+        }
+        const dw dd = dw_from(dv);
+        if (l == 11) gs.vxw = dd;
+        if (use_dw) {
+            switch (l) {
+                case 0: gs.Px = dd; break;
+                case 1: gs.Py = dd; break;
+                case 2: gs.nsx = dd; break;
+                case 3: gs.nsy = dd; break;
+                case 4: gs.tsx = dd; break;
+                case 5: gs.tsy = dd; break;
+                case 6: gs.T0 = dd; break;
+                case 7: gs.Tz = dd; break;
+                case 8: gs.inv_t = dd; break;
+                case 9: gs.inv_z = dd; break;
+                case 10: gs.Sw = dd; break;
+                default: break;
+            }
+        }
+        if (l == 12) {
             gs.inv_dt_f = (float)qv[4];
             gs.inv_dz_f = (float)qv[5];
             gs.inv_s = qv[6];
             gs.inv_x = qv[7];
-            if (use_dw) {
-                gs.T0 = dw_from(t - J.t_min);
-                gs.Tz = dw_from(t + J.z_min);
-                gs.inv_t = dw_from(qv[4]);
-                gs.inv_z = dw_from(qv[5]);
-                gs.Sw = dw_from(s);
-                gs.band_f = J.near_band > 0.0 ? (float)J.near_band : 0.f;
-            }
+            gs.band_f = (use_dw && J.near_band > 0.0) ? (float)J.near_band : 0.f;
         }
     } else {
         // warp 0: lane 0 finds the regions and the record layout, then one
@@ -485,14 +514,29 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
             gs.row_begin[gs.nreg] = rb;
         }
         __syncwarp();
+        // the regions' axes in one warp-wide division: lanes 0..3 the s'
+        // axis of region lane, lanes 4..7 the x' axis of region lane - 4
+        {
+            const int lane = threadIdx.x, rr = lane & 3;
+            const bool mine = lane < 8 && rr < gs.nreg;
+            double aa = 0.0, ab = 1.0;
+            int an = 2;
+            if (mine) {
+                const Region &R = gs.reg[rr];
+                if (lane < 4) { aa = R.sl; ab = R.sr; an = R.nsp; }
+                else { aa = R.xl; ab = R.xr; an = R.nxp; }
+            }
+            const Axis ax = make_axis(aa, ab, an);
+            if (mine) {
+                if (lane < 4) gs.ax_s[rr] = ax;
+                else { gs.ax_x[rr] = ax; gs.xref[rr] = ax.at(an / 2); }
+            }
+        }
+        __syncwarp();
         const int r = threadIdx.x;
         if (r < gs.nreg) {
             const Region &R = gs.reg[r];
-            const Axis A = make_axis(R.sl, R.sr, R.nsp);
-            const Axis AX = make_axis(R.xl, R.xr, R.nxp);
-            gs.ax_s[r] = A;
-            gs.ax_x[r] = AX;
-            gs.xref[r] = AX.at(R.nxp / 2);
+            const Axis A = gs.ax_s[r], AX = gs.ax_x[r];
             gs.lo[r] = R.nxp;
             gs.hi[r] = -1;
             // rho_at over the region's columns s'(j) = start + j step (non-
@@ -520,25 +564,45 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
             gs.wsf[r][1] = A.n < 2 ? 0.f : (float)A.step;
             gs.wxf[r][0] = AX.n < 2 ? 0.f : (float)(0.5 * AX.step);
             gs.wxf[r][1] = AX.n < 2 ? 0.f : (float)AX.step;
-            if (use_dw) {
-                gs.S0[r] = dw_from(A.start);
-                gs.Sst[r] = dw_from(A.step);
-                gs.X0[r] = dw_from(AX.start);
-                gs.Xst[r] = dw_from(AX.step);
-                gs.xrefw[r] = dw_from(gs.xref[r]);
-            }
         }
     }
     __syncthreads();
-    // orbit-table and history coordinates of the axes (need warp 1's
-    // reciprocals)
-    if (use_dw && threadIdx.x < gs.nreg) {
-        const int r = threadIdx.x;
-        const Axis A = gs.ax_s[r], AX = gs.ax_x[r];
-        gs.U0[r] = dw_from((A.start - J.s_min) * gs.inv_s);
-        gs.Ust[r] = dw_from(A.step * gs.inv_s);
-        gs.UX0[r] = dw_from((AX.start - J.x_min) * gs.inv_x);
-        gs.UXst[r] = dw_from(AX.step * gs.inv_x);
+    // the regions' double-word constants (nine per region; the orbit-table
+    // and history coordinates need warp 1's reciprocals), two warp-wide
+    // conversions: value v = 9 r + k
+    if (use_dw && threadIdx.x < 32) {
+        for (int v = threadIdx.x; v < 9 * WAKE_MAX_REGIONS; v += 32) {
+            const int r = v / 9, k = v - 9 * r;
+            double val = 0.0;
+            if (r < gs.nreg) {
+                const Axis A = gs.ax_s[r], AX = gs.ax_x[r];
+                switch (k) {
+                    case 0: val = A.start; break;
+                    case 1: val = A.step; break;
+                    case 2: val = AX.start; break;
+                    case 3: val = AX.step; break;
+                    case 4: val = gs.xref[r]; break;
+                    case 5: val = (A.start - J.s_min) * gs.inv_s; break;
+                    case 6: val = A.step * gs.inv_s; break;
+                    case 7: val = (AX.start - J.x_min) * gs.inv_x; break;
+                    default: val = AX.step * gs.inv_x; break;
+                }
+            }
+            const dw d = dw_from(val);
+            if (r < gs.nreg) {
+                switch (k) {
+                    case 0: gs.S0[r] = d; break;
+                    case 1: gs.Sst[r] = d; break;
+                    case 2: gs.X0[r] = d; break;
+                    case 3: gs.Xst[r] = d; break;
+                    case 4: gs.xrefw[r] = d; break;
+                    case 5: gs.U0[r] = d; break;
+                    case 6: gs.Ust[r] = d; break;
+                    case 7: gs.UX0[r] = d; break;
+                    default: gs.UXst[r] = d; break;
+                }
+            }
+        }
     }
     __syncthreads();
     // the finished record to global memory

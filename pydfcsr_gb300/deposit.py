@@ -116,7 +116,9 @@ class HistoryRing:
     def _alloc(self, cap):
         r64 = torch.empty((cap, self.nx, self.nz, 5), dtype=torch.float64,
                           device=self.device) if self.store64 else None
-        r32 = torch.zeros((cap, self.nx, self.nz, 8), dtype=torch.float32,
+        # no fill: the regrid writes all eight words of every cell of a slot
+        # (the two pad words as zeros) before the slot is read
+        r32 = torch.empty((cap, self.nx, self.nz, 8), dtype=torch.float32,
                           device=self.device) if self.store32 else None
         return r64, r32
 
