@@ -269,10 +269,12 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True, side
     ``events`` (list) receives one (start, end) CUDA event pair per step.
 
     ``side``: a second stream for the beam moments.  The particle sets are
-    resident before the loop, so step k+1's moments are enqueued once step
-    k's mesh is built, ahead of step k's wake: they run beside step k's DF
-    kernels instead of queueing behind the wake's persistent blocks, and the
-    host has step k+1's statistics while the GPU is still busy with step k."""
+    resident before the loop, so step k+1's moments are enqueued right after
+    step k's wake: their small CTAs fit beside the wake's persistent
+    integral CTAs and use the FP64 pipe the integral leaves idle (rather
+    than contending with the FP64-bound deposit, DF and set-up kernels), and
+    the host has step k+1's statistics while the GPU is still busy with step
+    k."""
     import torch
     csr = run.csr
     stream = torch.cuda.current_stream()
@@ -292,13 +294,12 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True, side
         if wake:
             csr.get_CSR_mesh()
             s, x = csr.mesh_device()
+        if wake:
+            run.last = csr.wake_device(s, x, precision)
         if k + 1 < first + count:
-            # the wake job below takes step k's statistics (set at the sync)
             run.beam.particle = sets[k]
             run.beam.update_status(stream=side, wait=False)
             pre = k + 1
-        if wake:
-            run.last = csr.wake_device(s, x, precision)
         if events is not None:
             ev[1].record(stream)
             events.append(ev)
@@ -331,11 +332,12 @@ def e2e_steps(run, host_sets, first, count, precision, dev_bufs, side):
     """Steps through the public API with host buffers: H2D of (x, px, z)
     from pinned memory, CSR2D calls, D2H of (dE_dct, x_kick).
 
-    Pipelined like a caller that streams beams through: once step k's mesh is
-    built, step k+1's upload and moments are enqueued on ``side`` into the
-    other of two device buffers, ahead of step k's wake on the main stream,
-    and step k's results (calculate_2D_CSR with wait=False) are read back
-    after step k+1 is enqueued."""
+    Pipelined like a caller that streams beams through: once step k's mesh
+    is built, step k+1's upload is enqueued on ``side`` into the other of two
+    device buffers (the copy engine overlaps step k's wake), and right after
+    step k's wake its moments (which run beside the wake's integral); step
+    k's results (calculate_2D_CSR with wait=False) are read back after step
+    k+1 is enqueued."""
     import torch
     csr = run.csr
     main = torch.cuda.current_stream()
@@ -352,16 +354,19 @@ def e2e_steps(run, host_sets, first, count, precision, dev_bufs, side):
             buf[0].copy_(xpz[0], non_blocking=True)
             buf[1].copy_(xpz[1], non_blocking=True)
             buf[4].copy_(xpz[2], non_blocking=True)
-        run.beam.particle = buf
-        run.beam.update_status(stream=side, wait=False)
-        ready[k % 2] = side.record_event()
         return xpz.numel() * 8
 
+    def moments(k):
+        run.beam.particle = dev_bufs[k % 2]
+        run.beam.update_status(stream=side, wait=False)
+        ready[k % 2] = side.record_event()
+
     pending = None
-    pre = None                    # step whose upload is already enqueued
+    pre = None                    # step whose upload and moments are already enqueued
     for k in range(first, first + count):
         if pre != k:
             h2d += upload(k)
+            moments(k)
         run.beam.sync_status()
         main.wait_event(ready[k % 2])
         run.beam.position = float(run.plan.positions[k])
@@ -371,8 +376,10 @@ def e2e_steps(run, host_sets, first, count, precision, dev_bufs, side):
         csr.get_CSR_mesh()
         if k + 1 < first + count:
             h2d += upload(k + 1)
-            pre = k + 1
         nxt = csr.calculate_2D_CSR(precision, wait=False)
+        if k + 1 < first + count:
+            moments(k + 1)
+            pre = k + 1
         if pending is not None:
             dE, xk = pending.result()               # step k-1 on the host
             d2h += dE.nbytes + xk.nbytes
@@ -404,10 +411,9 @@ def gpu_arm(a):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # warm-up (builds the history; untimed).  The side stream (next step's
-    # moments, uploads) has the highest priority: its blocks are scheduled as
-    # soon as an SM frees, rather than behind the queued wake blocks
-    side = torch.cuda.Stream(priority=-5)
+    # warm-up (builds the history; untimed); the side stream carries the next
+    # step's moments (and uploads)
+    side = torch.cuda.Stream()
     timed_steps(run, sets, 1, W, a.precision, side=side)
     barrier()
     fma_peaks = measure_fma_peaks()

@@ -24,7 +24,10 @@ namespace dfcsr {
 //           x - mean_x) and x_transform = x - (slope z + intercept) (sum and
 //           square sum) -> sigma_x of the slice, mean and sigma of x_transform.
 // FP64 operations per particle: 7 in pass 1, 8 in pass 2.
-constexpr int MOM_THREADS = 256;
+// 128-thread CTAs of 32 registers: one fits beside the wake's persistent
+// integral CTAs (which leave 4096 registers per SM), so the next step's
+// moments can run during the integral on the FP64 pipe it leaves idle
+constexpr int MOM_THREADS = 128;
 constexpr int MOM_MAX_BLOCKS = 1024;
 constexpr int MOM_K = 5;   // partial sums per pass
 
