@@ -477,21 +477,43 @@ __global__ void seg_combine(const uint32_t *__restrict__ cstart, const uint32_t 
     const double *first = (cs == t0 * SEG_K) ? chunk_first : chunk_last;
 #pragma unroll
     for (int c = 0; c < 8; ++c) acc[c] = first[(size_t)t0 * 8 + c];
-    // same order of additions; unrolled so the loads of later chunks are in
-    // flight while earlier ones are added
-#pragma unroll 4
-    for (uint32_t t = t0 + 1; t <= t1; ++t) {
-        const double2 *src = reinterpret_cast<const double2 *>(chunk_first + (size_t)t * 8);
-        const double2 v0 = src[0], v1 = src[1], v2 = src[2], v3 = src[3];
-        acc[0] = __dadd_rn(acc[0], v0.x);
-        acc[1] = __dadd_rn(acc[1], v0.y);
-        acc[2] = __dadd_rn(acc[2], v1.x);
-        acc[3] = __dadd_rn(acc[3], v1.y);
-        acc[4] = __dadd_rn(acc[4], v2.x);
-        acc[5] = __dadd_rn(acc[5], v2.y);
-        acc[6] = __dadd_rn(acc[6], v3.x);
-        acc[7] = __dadd_rn(acc[7], v3.y);
+    // the later chunks' parts in four interleaved partial sums (chunk t goes
+    // to sum (t - t0 - 1) % 4), then ((acc + s0) + s1) + (s2 + s3): a dense
+    // cell spans tens of chunks, and a running sum would be a chain of that
+    // many dependent FP64 additions (some hundred cycles each on this GPU)
+    double ps[4][8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) ps[q][c] = 0.0;
+    uint32_t t = t0 + 1;
+    for (; t + 3 <= t1; t += 4) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double2 *src = reinterpret_cast<const double2 *>(chunk_first + (size_t)(t + q) * 8);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const double2 v = src[h];
+                ps[q][2 * h] = __dadd_rn(ps[q][2 * h], v.x);
+                ps[q][2 * h + 1] = __dadd_rn(ps[q][2 * h + 1], v.y);
+            }
+        }
     }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        if (t + q <= t1) {
+            const double2 *src = reinterpret_cast<const double2 *>(chunk_first + (size_t)(t + q) * 8);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const double2 v = src[h];
+                ps[q][2 * h] = __dadd_rn(ps[q][2 * h], v.x);
+                ps[q][2 * h + 1] = __dadd_rn(ps[q][2 * h + 1], v.y);
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+        acc[c] = __dadd_rn(__dadd_rn(__dadd_rn(acc[c], ps[0][c]), ps[1][c]), __dadd_rn(ps[2][c], ps[3][c]));
     store8(partial + (size_t)k * 8, acc);
 }
 
