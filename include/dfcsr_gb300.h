@@ -83,8 +83,9 @@ int dfcsr_beam_moments(const double *x, const double *z, int64_t n, double *out,
  * 1 - frac, bounds-checked corners - exactly the reference's rule.
  * Deterministic: particles are sorted by lower cell (stable LSD radix sort);
  * fixed-size chunks of the sorted particles are summed per cell and the
- * parts of cells that cross chunks are added in chunk order.  No float
- * atomics; the order of additions depends only on the input order.
+ * parts of cells that cross chunks are added in a fixed order (four
+ * interleaved partial sums over the chunks).  No float atomics; the order
+ * of additions depends only on the input order.
  * Needs dfcsr_deposit_workspace_bytes(n, nb1, nb2) bytes of scratch.
  */
 size_t dfcsr_deposit_workspace_bytes(int64_t n, int nb1, int nb2);
