@@ -41,6 +41,10 @@ int dfcsr_version(void);
 const char *dfcsr_last_error(void);
 /* Short name of a status code. */
 const char *dfcsr_status_name(int status);
+/* Number of kernel launches this library has issued in this process (all
+ * entry points, all devices; launches recorded into a CUDA graph count once,
+ * at capture).  Host-side counter, no device synchronisation. */
+long long dfcsr_kernel_launches(void);
 /* sizeof of the ABI structs: 0 dfcsr_df_params, 1 dfcsr_wake_job (for
  * bindings that lay the structs out themselves); 0 for other values. */
 size_t dfcsr_abi_sizeof(int which);

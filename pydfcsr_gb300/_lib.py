@@ -97,6 +97,7 @@ class WakeJob(ctypes.Structure):
 # (name, restype, argtypes)
 _SIGS = [
     ("dfcsr_version", _c_int, []),
+    ("dfcsr_kernel_launches", ctypes.c_longlong, []),
     ("dfcsr_last_error", ctypes.c_char_p, []),
     ("dfcsr_status_name", ctypes.c_char_p, [_c_int]),
     ("dfcsr_abi_sizeof", _c_size, [_c_int]),
@@ -186,6 +187,11 @@ def call(name, *args):
 def query(name, *args):
     """Call a size / info function (no status)."""
     return getattr(load(), name)(*args)
+
+
+def kernel_launches():
+    """Kernel launches issued by the library so far in this process."""
+    return int(load().dfcsr_kernel_launches())
 
 
 def timing_enable(on=True):

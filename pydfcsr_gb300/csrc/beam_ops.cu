@@ -118,6 +118,7 @@ extern "C" int dfcsr_transport6(const double *R, double *coords, int64_t n, int6
     Matrix6 M;
     for (int k = 0; k < 36; ++k) M.m[k] = R[k];
     ScopedTiming tm("transport6", as_stream(stream));
+    note_launch();
     transport6<<<(unsigned)((n + 255) / 256), 256, 0, as_stream(stream)>>>(M, coords, n, ld);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
@@ -149,9 +150,11 @@ extern "C" int dfcsr_apply_wakes(double *coords, int64_t n, int64_t ld, const do
     cudaStream_t st = as_stream(stream);
     double *tables = reinterpret_cast<double *>(workspace);
     ScopedTiming tm("apply_wakes", st);
+    note_launch();
     scale_kicks<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(
         dE_dct, transverse_on ? x_kick : nullptr, cells, step_size, init_energy, tables);
     const size_t smem = (size_t)(nx + nz) * sizeof(double);
+    note_launch();
     apply_kicks<<<(unsigned)((n + 255) / 256), 256, smem, st>>>(
         coords, n, ld, tables, cells, transverse_on ? 1 : 0, xrange, zrange, nx, nz, slope0, slope1);
     DFCSR_LAUNCH_CHECK();

@@ -2,6 +2,8 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <atomic>
+
 #include "dfcsr_common.cuh"
 
 namespace dfcsr {
@@ -17,6 +19,10 @@ void set_error(const char *fmt, ...) {
 
 void clear_error() { g_msg[0] = '\0'; }
 
+static std::atomic<long long> g_launches{0};
+
+void note_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
 int num_sms() {
     int dev = 0, n = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 148;
@@ -27,6 +33,8 @@ int num_sms() {
 }  // namespace dfcsr
 
 extern "C" int dfcsr_version(void) { return 100; }
+
+extern "C" long long dfcsr_kernel_launches(void) { return dfcsr::g_launches.load(); }
 
 extern "C" const char *dfcsr_last_error(void) { return dfcsr::g_msg; }
 

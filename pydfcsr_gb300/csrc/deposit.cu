@@ -606,9 +606,13 @@ extern "C" int dfcsr_beam_moments(const double *x, const double *z, int64_t n, d
     double *part = reinterpret_cast<double *>(workspace);
     ScopedTiming tm("beam_moments", s);
     DFCSR_CUDA_TRY(cudaMemsetAsync(out, 0, 16 * sizeof(double), s));
+    note_launch();
     moments_pass<1><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
+    note_launch();
     moments_finish<1><<<1, MOM_THREADS, 0, s>>>(x, z, part, nblk, n, out);
+    note_launch();
     moments_pass<2><<<nblk, MOM_THREADS, 0, s>>>(x, z, n, out, part);
+    note_launch();
     moments_finish<2><<<1, MOM_THREADS, 0, s>>>(x, z, part, nblk, n, out);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
@@ -655,18 +659,23 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
     ScopedTiming tm("deposit_cic2d", s);
     if (n > 0) {
         const int tb = 256;
+        note_launch();
         cic_keys<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(q1, q2, n, nb1, start1, inv1, nb2,
                                                               start2, inv2, L.nkeys, ka, va);
         uint32_t *kin = ka, *vin = va, *kout = kb, *vout = vb;
         for (int p = 0; p < L.passes; ++p) {
             const int shift = RS_BITS * p;
+            note_launch();
             radix_upsweep<<<L.ntiles, RS_THREADS, 0, s>>>(kin, n, shift, L.ntiles, hist);
+            note_launch();
             radix_scan_rows<<<RS_BINS, 1024, 0, s>>>(hist, L.ntiles, dtot);
+            note_launch();
             radix_scatter<<<L.ntiles, RS_THREADS, sizeof(ScatterSmem), s>>>(kin, vin, n, shift, L.ntiles,
                                                                              hist, dtot, kout, vout);
             uint32_t *t = kin; kin = kout; kout = t;
             t = vin; vin = vout; vout = t;
         }
+        note_launch();
         cell_ranges<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(kin, n, cs, ce);
         double *cfirst = reinterpret_cast<double *>(kout);
         double *clast = reinterpret_cast<double *>(vout);
@@ -674,17 +683,20 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
 #define DFCSR_SEG(A, B)                                                                       \
     seg_sums<A, B><<<sb, SEG_THREADS, 0, s>>>(kin, vin, n, L.nkeys, nb2, cs, ce, q1, q2, w0, w1, \
                                               start1, inv1, start2, inv2, part, cfirst, clast)
+        note_launch();
         if (w0 && w1) DFCSR_SEG(true, true);
         else if (w0) DFCSR_SEG(true, false);
         else if (w1) DFCSR_SEG(false, true);
         else DFCSR_SEG(false, false);
 #undef DFCSR_SEG
+        note_launch();
         seg_combine<<<(unsigned)((L.nkeys + 255) / 256), 256, 0, s>>>(cs, ce, L.nkeys, cfirst,
                                                                        clast, part);
     } else {
         DFCSR_CUDA_TRY(cudaMemsetAsync(part, 0, sizeof(double) * (size_t)L.nkeys * 8, s));
     }
     const int64_t cells = (int64_t)nb1 * nb2;
+    note_launch();
     cic_assemble<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(part, nb1, nb2, out0, out1);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;

@@ -59,6 +59,10 @@ struct Carver {
 
 int num_sms();
 
+// Host-side count of kernel launches issued by this library (defined in
+// capi.cu; read through dfcsr_kernel_launches).
+void note_launch(int k = 1);
+
 // Kernel timing hooks (capi.cu): no-ops unless dfcsr_timing_enable(1).
 bool timing_on();
 void timing_begin(const char *name, cudaStream_t s, void **token);

@@ -526,6 +526,7 @@ extern "C" int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, doub
     ScopedTiming tm("df_finalize", s);
     DFCSR_CUDA_TRY(cudaMemsetAsync(A.bar, 0, sizeof(GridBar), s));
     void *args[] = {&A};
+    note_launch();
     DFCSR_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)df_stage, dim3(blocks), dim3(DF_THREADS), args,
                                                (size_t)smem, s));
     DFCSR_LAUNCH_CHECK();

@@ -142,6 +142,7 @@ extern "C" int dfcsr_rgi_axis_linspace(double src_start, double src_stop, int ns
     DFCSR_CHECK_ARG(nsrc >= 2 && ntgt >= 1, "dfcsr_rgi_axis_linspace: need nsrc >= 2, ntgt >= 1");
     DFCSR_CHECK_ARG(idx && w && oob, "dfcsr_rgi_axis_linspace: null pointer");
     DFCSR_CHECK_ARG(src_stop > src_start, "dfcsr_rgi_axis_linspace: source grid must ascend");
+    note_launch();
     rgi_axis_linspace<<<(unsigned)((ntgt + 127) / 128), 128, 0, as_stream(stream)>>>(
         src_start, src_stop, nsrc, tgt_start, tgt_stop, ntgt, idx, w, oob);
     DFCSR_LAUNCH_CHECK();
@@ -167,6 +168,7 @@ extern "C" int dfcsr_history_regrid(const double *density, const double *density
     const int64_t cells = (int64_t)nxi * nzi;
     ScopedTiming tm("history_regrid", as_stream(stream));
     const unsigned blocks = (unsigned)((cells + 255) / 256);
+    note_launch();
     if (ring64_slot)
         regrid5<true><<<blocks, 256, 0, as_stream(stream)>>>(
             density, density_x, density_z, vx, vx_x, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,

@@ -74,6 +74,7 @@ extern "C" int dfcsr_csr_mesh(double x0, double x1, int xbins, double z0, double
     DFCSR_CHECK_ARG(xbins >= 1 && zbins >= 1, "dfcsr_csr_mesh: empty mesh (%d x %d)", xbins, zbins);
     DFCSR_CHECK_ARG(s && x, "dfcsr_csr_mesh: null pointer");
     const int64_t n = (int64_t)xbins * zbins;
+    note_launch();
     csr_mesh_kernel<<<(unsigned)((n + 255) / 256), 256, 0, as_stream(stream)>>>(
         x0, x1, xbins, z0, z1, zbins, slope0, slope1, position, s, x);
     DFCSR_LAUNCH_CHECK();
@@ -89,6 +90,7 @@ extern "C" int dfcsr_interp3d(const double *qt, const double *qx, const double *
     if (m == 0) return DFCSR_OK;
     DFCSR_CHECK_ARG(qt && qx && qz && data && out, "dfcsr_interp3d: null pointer");
     DFCSR_CHECK_ARG(nt >= 1 && nx >= 1 && nz >= 1, "dfcsr_interp3d: empty grid");
+    note_launch();
     interp3d_kernel<<<(unsigned)((m + 255) / 256), 256, 0, as_stream(stream)>>>(
         qt, qx, qz, m, data, nt, nx, nz, min_t, min_x, min_z, delta_t, delta_x, delta_z, out);
     DFCSR_LAUNCH_CHECK();
@@ -102,6 +104,7 @@ extern "C" int dfcsr_interp1d(const double *q, int64_t m, const double *table, i
     if (m == 0) return DFCSR_OK;
     DFCSR_CHECK_ARG(q && table && out, "dfcsr_interp1d: null pointer");
     DFCSR_CHECK_ARG(n >= 1, "dfcsr_interp1d: empty table");
+    note_launch();
     interp1d_kernel<<<(unsigned)((m + 255) / 256), 256, 0, as_stream(stream)>>>(q, m, table, n, min_x,
                                                                                 delta_x, out);
     DFCSR_LAUNCH_CHECK();

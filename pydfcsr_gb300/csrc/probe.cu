@@ -39,6 +39,7 @@ extern "C" int dfcsr_probe_fma(int fp64, int64_t iters, void *sink, double *flop
     const int blocks = PROBE_BLOCKS_PER_SM * num_sms();
     *flops = 2.0 * PROBE_CHAINS * (double)iters * (double)blocks * PROBE_THREADS;
     cudaStream_t st = as_stream(stream);
+    note_launch();
     if (fp64)
         fma_probe<double><<<blocks, PROBE_THREADS, 0, st>>>(iters, 0.999999, 1e-7,
                                                             reinterpret_cast<double *>(sink));

@@ -125,6 +125,7 @@ extern "C" int dfcsr_wake_integrand(const dfcsr_wake_job *job, double s, double 
     DFCSR_CHECK_ARG(m >= 0, "dfcsr_wake_integrand: negative point count");
     if (m == 0) return DFCSR_OK;
     DFCSR_CHECK_ARG(job && sp && xp && Iz && Ix, "dfcsr_wake_integrand: null pointer");
+    note_launch();
     integrand_points<<<(unsigned)((m + 127) / 128), 128, 0, as_stream(stream)>>>(job, s, x, sp, xp, m,
                                                                                   ignore_vx, Iz, Ix);
     DFCSR_LAUNCH_CHECK();
@@ -141,6 +142,7 @@ extern "C" int dfcsr_wake_fp64(const dfcsr_wake_job *jobs, const int32_t *job_of
     cudaStream_t st = as_stream(stream);
     const int64_t grid64 = n < (int64_t)(1 << 30) ? n : (int64_t)(1 << 30);
     ScopedTiming tm("wake_fp64", st);
+    note_launch();
     wake_fp64_kernel<<<(unsigned)grid64, F64_THREADS, 0, st>>>(jobs, job_of_point, s, x, n, dE, xkick);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;

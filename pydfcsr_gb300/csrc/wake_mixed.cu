@@ -1151,9 +1151,11 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
             if (first + count > setup_first + setup_count) {   // next set-up chunk
                 setup_first = first;
                 setup_count = (n - first < L.setup_pts) ? n - first : L.setup_pts;
+                note_launch();
                 mixed_setup<<<(unsigned)setup_count, SETUP_THREADS, 0, st>>>(
                     jobs, job_of_point, s, x, setup_first, setup_count, L.rec_words, max_rows, setup);
             }
+            note_launch();
             mixed_geometry<<<(unsigned)count, GEO_THREADS, 0, st>>>(
                 jobs, job_of_point, s, x, first, count, setup + (first - setup_first), L.rec_words, rec,
                 meta, rows, obs_vx);
@@ -1161,14 +1163,17 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
         const int blocks = (int)((int64_t)blocks_max < count ? blocks_max : count);
         {
             ScopedTiming tm("wake_mixed_integral", st);
+            note_launch();
             mixed_integral<<<blocks, MX_THREADS, smem, st>>>(
                 jobs, job_of_point, first, count, L.rec_words, rec, meta, rows, part, counter);
         }
         if (use_band) {
             ScopedTiming tm("wake_mixed_band", st);
+            note_launch();
             mixed_band<<<dim3((unsigned)count, WAKE_MAX_REGIONS), 128, 0, st>>>(
                 jobs, job_of_point, s, x, first, count, meta, obs_vx, band);
         }
+        note_launch();
         mixed_finalize<<<(unsigned)((count + 127) / 128), 128, 0, st>>>(
             jobs, job_of_point, first, count, meta, part, use_band ? band : nullptr, dE, xkick);
     }

@@ -35,6 +35,15 @@ def test_every_header_symbol_exported():
     assert set(names) <= set(_lib.EXPORTS), set(names) - set(_lib.EXPORTS)
 
 
+def test_launch_counter_without_gpu():
+    """The launch counter is host-side: readable without a device, and an
+    argument error launches nothing."""
+    n0 = _lib.kernel_launches()
+    with pytest.raises(_lib.DfcsrBadArgument):
+        _lib.call("dfcsr_csr_mesh", 0.0, 1.0, 0, 0.0, 1.0, 4, 0.0, 0.0, 0.0, None, None, None)
+    assert _lib.kernel_launches() == n0
+
+
 def test_struct_layouts_match():
     lib = _lib.load()
     assert lib.dfcsr_abi_sizeof(0) == ctypes.sizeof(_lib.DFParams)

@@ -355,3 +355,9 @@ def test_calculate_2d_csr_nonblocking_matches_blocking():
     assert np.array_equal(dE0, dE1) and np.array_equal(xk0, xk1)
     csr.calculate_2D_CSR("mixed", wait=False)
     assert np.array_equal(csr.dE_dct, dE0) and np.array_equal(csr.x_kick, xk0)
+    # the library's launch counter sees the mesh kernel and the wake's set-up,
+    # geometry, integral and finalize launches (one batch here)
+    from pydfcsr_gb300 import _lib
+    n0 = _lib.kernel_launches()
+    csr.calculate_2D_CSR("mixed")
+    assert _lib.kernel_launches() - n0 == 5
