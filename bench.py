@@ -268,38 +268,54 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True, side
     """Run steps first..first+count-1 from device-resident particle sets;
     ``events`` (list) receives one (start, end) CUDA event pair per step.
 
-    ``side``: a second stream for the beam moments.  The particle sets are
-    resident before the loop, so step k+1's moments are enqueued right after
-    step k's wake: their small CTAs fit beside the wake's persistent
-    integral CTAs and use the FP64 pipe the integral leaves idle (rather
-    than contending with the FP64-bound deposit, DF and set-up kernels), and
-    the host has step k+1's statistics while the GPU is still busy with step
-    k."""
+    Pipelined across steps (the particle sets are resident, and without kicks
+    a step's particles do not depend on the previous wake), with ``side`` a
+    second stream:
+    * the moments of step k+2 are enqueued on ``side`` right after step k's
+      wake: their small CTAs run beside the wake's persistent integral CTAs,
+      on the FP64 pipe the integral leaves idle;
+    * the deposit of step k+1 is enqueued on ``side`` when step k begins
+      (its moments are on the host by then): it runs beside step k's DF
+      finalisation, regrid, set-up and geometry kernels, which leave SMs
+      free;
+    * step k's DF finalisation, history and wake go to the main stream."""
     import torch
-    csr = run.csr
+    csr, beam = run.csr, run.beam
+    trk = csr.DF_tracker
+    side = side if side is not None else torch.cuda.current_stream()
     stream = torch.cuda.current_stream()
-    pre = None                      # step whose moments are already enqueued
-    for k in range(first, first + count):
+    last = first + count - 1
+
+    def status(k):                   # moments of step k (on side)
+        beam.particle = sets[k - 1]
+        return beam.status_async(side)
+
+    def deposit(k, st):              # deposit of step k (on side)
+        p = sets[k - 1]
+        return trk.deposit_DF(p[0], p[4], p[1], st.result(), side)
+
+    st = {first: status(first)}
+    if first + 1 <= last:
+        st[first + 1] = status(first + 1)
+    dep = {first: deposit(first, st[first])}
+    for k in range(first, last + 1):
         if events is not None:
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record(stream)
-        if pre != k:
-            run.beam.particle = sets[k - 1]
-            run.beam.update_status(stream=side, wait=False)
-        run.beam.sync_status()
-        run.beam.position = float(run.plan.positions[k])
-        run.beam.step = k
-        lf = run.plan.formation_length(k, run.beam.sigma_z)
-        csr.update_history(lf)
+        if k + 1 <= last:
+            dep[k + 1] = deposit(k + 1, st[k + 1])
+        beam.particle = sets[k - 1]
+        beam.apply_status(st.pop(k))
+        beam.position = float(run.plan.positions[k])
+        beam.step = k
+        lf = run.plan.formation_length(k, beam.sigma_z)
+        csr.update_history(lf, deposited=dep.pop(k))
         if wake:
             csr.get_CSR_mesh()
             s, x = csr.mesh_device()
-        if wake:
             run.last = csr.wake_device(s, x, precision)
-        if k + 1 < first + count:
-            run.beam.particle = sets[k]
-            run.beam.update_status(stream=side, wait=False)
-            pre = k + 1
+        if k + 2 <= last:
+            st[k + 2] = status(k + 2)
         if events is not None:
             ev[1].record(stream)
             events.append(ev)

@@ -173,15 +173,19 @@ class CSR2D:
         else:
             self.formation_length = (3 * R ** 2 * phi ** 4) / (4 * (-6 * sigma_z + R * phi ** 3))
 
-    def update_history(self, formation_length=None):
-        """The per-step DF calls of CSR2D.run (CSR.py:297-307)."""
+    def update_history(self, formation_length=None, deposited=None):
+        """The per-step DF calls of CSR2D.run (CSR.py:297-307).
+
+        ``deposited`` (extension): a :meth:`DF_tracker.deposit_DF` handle for
+        this step's particles, enqueued earlier (e.g. on another stream while
+        the previous step ran); the deposit is then not repeated."""
         if formation_length is not None:
             self.formation_length = formation_length
         b = self.beam
         b.sync_status()
         t = self.DF_tracker
         # the beam's moments are of these same (x, z) tensors
-        t.get_DF(x=b.x, z=b.z, px=b.px, t=b.position, moments=b._moments)
+        t.get_DF(x=b.x, z=b.z, px=b.px, t=b.position, moments=b._moments, deposited=deposited)
         t.append_DF()
         t.append_interpolant(formation_length=self.formation_length,
                              n_formation_length=self.integration_params.n_formation_length)

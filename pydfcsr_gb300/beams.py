@@ -21,6 +21,20 @@ from .runtime import as_device_f64, default_workspace, ptr, require_cuda, stream
 __all__ = ["Beam"]
 
 
+class PendingStatus:
+    """Beam moments in flight (see :meth:`Beam.status_async`): the device
+    array, its pinned host copy and the event after the copy."""
+    __slots__ = ("device", "host", "event")
+
+    def __init__(self, device, host, event):
+        self.device, self.host, self.event = device, host, event
+
+    def result(self):
+        """The 16 moments as a numpy array (waits for the copy)."""
+        self.event.synchronize()
+        return self.host.numpy().copy()
+
+
 class Beam:
     def __init__(self, coords, charge=1e-9, energy=1e9, position=0.0, workspace=None,
                  adopt=False):
@@ -52,12 +66,12 @@ class Beam:
             self.particle = self.particle.clone()
             self._owned = True
 
-    def update_status(self, stream=None, wait=True):
-        """Beam statistics from one device moments call; waits for it (and
-        for whatever precedes it on ``stream``, default the current one).
-
-        ``wait=False`` only enqueues the moments and their copy to pinned host
-        memory; :meth:`sync_status` (or the next update) completes them."""
+    def status_async(self, stream=None):
+        """(extension) Enqueue the moments of the current particles and their
+        copy to pinned host memory on ``stream`` (default: the current one);
+        returns a :class:`PendingStatus`.  The beam's statistics change only
+        when the handle is applied (:meth:`apply_status`), so the moments of
+        later particle sets can be in flight while these are in use."""
         s = stream if stream is not None else torch.cuda.current_stream()
         with torch.cuda.stream(s):
             m = beam_moments(self.particle[0], self.particle[4], ws=self.ws)
@@ -65,24 +79,36 @@ class Beam:
             host.copy_(m, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(s)
-        self._moments_dev = m
-        self._pending_status = (host, ev)
+        return PendingStatus(m, host, ev)
+
+    def apply_status(self, pending):
+        """Set the statistics from a :meth:`status_async` handle (waits for
+        its copy)."""
+        st = pending.result()
+        self._moments_dev = pending.device
+        self._moments = st
+        self._mean_x, self._mean_z = float(st[1]), float(st[2])
+        self._sigma_x, self._sigma_z = float(st[3]), float(st[4])
+        self._slope = np.array([st[5], st[6]])
+
+    def update_status(self, stream=None, wait=True):
+        """Beam statistics from one device moments call; waits for it (and
+        for whatever precedes it on ``stream``, default the current one).
+
+        ``wait=False`` only enqueues the moments and their copy to pinned host
+        memory; :meth:`sync_status` (or the next update) completes them."""
+        self._pending_status = self.status_async(stream)
         if wait:
             self.sync_status()
 
     def sync_status(self):
         """Wait for the moments enqueued by ``update_status(wait=False)`` and
         set the statistics from them."""
-        if getattr(self, "_pending_status", None) is None:
+        pending = getattr(self, "_pending_status", None)
+        if pending is None:
             return
-        host, ev = self._pending_status
-        ev.synchronize()
         self._pending_status = None
-        st = host.numpy().copy()
-        self._moments = st
-        self._mean_x, self._mean_z = float(st[1]), float(st[2])
-        self._sigma_x, self._sigma_z = float(st[3]), float(st[4])
-        self._slope = np.array([st[5], st[6]])
+        self.apply_status(pending)
 
     def transport(self, R):
         """coords <- R coords in place (6x6 FP64 matrix, e.g. from r_gen6)."""

@@ -186,7 +186,7 @@ radix_scan_rows(uint32_t *__restrict__ hist, int ntiles, uint32_t *__restrict__ 
     if (threadIdx.x == 0) carry_s = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int off = 0; off < ntiles; off += 1024) {
+    for (int off = 0; off < ntiles; off += blockDim.x) {
         const int i = off + threadIdx.x;
         const uint32_t v = (i < ntiles) ? row[i] : 0u;
         uint32_t inc = v;
@@ -209,7 +209,7 @@ radix_scan_rows(uint32_t *__restrict__ hist, int ntiles, uint32_t *__restrict__ 
         const uint32_t carry = carry_s;
         if (i < ntiles) row[i] = carry + wsum[warp] + inc - v;
         __syncthreads();
-        if (threadIdx.x == 1023) carry_s = carry + wsum[warp] + inc;
+        if (threadIdx.x == blockDim.x - 1) carry_s = carry + wsum[warp] + inc;
         __syncthreads();
     }
     if (threadIdx.x == 0) dtot[blockIdx.x] = carry_s;

@@ -175,6 +175,16 @@ class HistoryRing:
         return self.ring32[idx][..., f].double().cpu().numpy()
 
 
+class PendingDeposit:
+    """A deposit enqueued by :meth:`DF_tracker.deposit_DF`: the host moments
+    it was sized from, the field array [5, nx, nz] (channels 0 and 3 written
+    by the deposit) and the event recorded after it."""
+    __slots__ = ("moments", "fields", "event")
+
+    def __init__(self, moments, fields, event):
+        self.moments, self.fields, self.event = moments, fields, event
+
+
 class _DFEntry:
     """One logged DF: grids (numpy linspaces and their (start, stop, n)),
     the five fields on the device, the finalisation scalars, t and sigmas."""
@@ -245,39 +255,72 @@ class DF_tracker:
     def _workspace(self):
         return self.ws or default_workspace()
 
-    def get_DF(self, x, z, px, t, stream=None, moments=None):
-        """Deposit and finalise the current DF (deposit.py:145-245).
-
-        ``moments`` (extension): the host copy of ``beam_moments(x, z)`` when
-        the caller already has it for these exact arrays (saves a pass and a
-        device synchronisation)."""
-        require_cuda()
-        xd, zd, pxd = (as_device_f64(a).reshape(-1) for a in (x, z, px))
-        ws = self._workspace()
-        if moments is None:
-            st = beam_moments(xd, zd, stream, ws).cpu().numpy()
-        else:
-            st = np.asarray(moments, dtype=np.float64)
-        self.stats = st
+    def _grid(self, st):
+        """Grid and smoothing window of get_DF (deposit.py:157-170) from the
+        beam moments ``st`` (host array of dfcsr_beam_moments)."""
         sigma_x, sigma_z = float(st[3]), float(st[4])
-        self.sigma_x, self.sigma_z = sigma_x, sigma_z
-        self.xmean, self.zmean = float(st[1]), float(st[2])
+        xmean, zmean = float(st[1]), float(st[2])
         with np.errstate(all="ignore"):
             frac = np.float64(sigma_x) / np.float64(st[8])
         if frac > 5 or self.grid_rule == "configured":
             xb, zb, win = int(self.xbins), int(self.zbins), int(self.filter_window)
         else:
             xb, zb, win = 100, 100, 5
-        x0 = self.xmean - self.xlim * sigma_x
-        x1 = self.xmean + self.xlim * sigma_x
-        z0 = self.zmean - self.zlim * sigma_z
-        z1 = self.zmean + self.zlim * sigma_z
+        x0 = xmean - self.xlim * sigma_x
+        x1 = xmean + self.xlim * sigma_x
+        z0 = zmean - self.zlim * sigma_z
+        z1 = zmean + self.zlim * sigma_z
+        return xb, zb, win, x0, x1, z0, z1
+
+    def deposit_DF(self, x, z, px, moments, stream=None):
+        """(extension) The deposit half of get_DF, for particles whose host
+        moments are already known: the grid from ``moments``, both CIC
+        channels into a new field array, enqueued on ``stream`` (default:
+        the current stream).  Returns a :class:`PendingDeposit` to hand to
+        ``get_DF(..., deposited=...)``; the tracker's state is not touched,
+        so the deposit of a later step can run while this step is finalised.
+        ``x``, ``z``, ``px`` must stay unchanged until the deposit has run."""
+        require_cuda()
+        st = np.asarray(moments, dtype=np.float64)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        xb, zb, win, x0, x1, z0, z1 = self._grid(st)
+        with torch.cuda.stream(s):
+            xd, zd, pxd = (as_device_f64(a).reshape(-1) for a in (x, z, px))
+            fields = torch.empty((5, xb, zb), dtype=torch.float64, device=xd.device)
+            deposit_cic(xd, zd, None, pxd, xb, x0, x1, zb, z0, z1, s, self._workspace(),
+                        out0=fields[0], out1=fields[3])
+            ev = torch.cuda.Event()
+            ev.record(s)
+        return PendingDeposit(st, fields, ev)
+
+    def get_DF(self, x, z, px, t, stream=None, moments=None, deposited=None):
+        """Deposit and finalise the current DF (deposit.py:145-245).
+
+        ``moments`` (extension): the host copy of ``beam_moments(x, z)`` when
+        the caller already has it for these exact arrays (saves a pass and a
+        device synchronisation).  ``deposited`` (extension): the handle of an
+        earlier :meth:`deposit_DF` of these particles; the deposit is then
+        not repeated (x, z, px are not read) and ``stream`` waits for it."""
+        require_cuda()
+        ws = self._workspace()
+        if deposited is None:
+            if moments is None:
+                xd, zd = (as_device_f64(a).reshape(-1) for a in (x, z))
+                moments = beam_moments(xd, zd, stream, ws).cpu().numpy()
+            deposited = self.deposit_DF(x, z, px, moments, stream)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        s.wait_event(deposited.event)
+        fields = deposited.fields
+        fields.record_stream(s)
+        st = deposited.moments
+        self.stats = st
+        sigma_x, sigma_z = float(st[3]), float(st[4])
+        self.sigma_x, self.sigma_z = sigma_x, sigma_z
+        self.xmean, self.zmean = float(st[1]), float(st[2])
+        xb, zb, win, x0, x1, z0, z1 = self._grid(st)
         xg = np.linspace(x0, x1, xb)
         zg = np.linspace(z0, z1, zb)
-        fields = torch.empty((5, xb, zb), dtype=torch.float64, device=xd.device)
-        deposit_cic(xd, zd, None, pxd, xb, x0, x1, zb, z0, z1, stream, ws, out0=fields[0],
-                    out1=fields[3])
-        sc = torch.empty(8, dtype=torch.float64, device=xd.device)   # written by df_finalize
+        sc = torch.empty(8, dtype=torch.float64, device=fields.device)   # written by df_finalize
         self._finalize(fields, sc, xg, zg, win, stream, ws)
         self.x_grids, self.z_grids = xg, zg
         self._cur = _DFEntry(xg, zg, fields, sc, t, sigma_x, sigma_z, (x0, x1, xb), (z0, z1, zb))
