@@ -348,54 +348,67 @@ def e2e_steps(run, host_sets, first, count, precision, dev_bufs, side):
     """Steps through the public API with host buffers: H2D of (x, px, z)
     from pinned memory, CSR2D calls, D2H of (dE_dct, x_kick).
 
-    Pipelined like a caller that streams beams through: once step k's mesh
-    is built, step k+1's upload is enqueued on ``side`` into the other of two
-    device buffers (the copy engine overlaps step k's wake), and right after
-    step k's wake its moments (which run beside the wake's integral); step
-    k's results (calculate_2D_CSR with wait=False) are read back after step
-    k+1 is enqueued."""
+    Pipelined like timed_steps, for a caller that streams beams through
+    three device buffers: step k+2's upload goes to a copy stream when step
+    k begins (once step k-1's deposit has released that buffer), its moments
+    to ``side`` right after step k's wake, step k+1's deposit to ``side``
+    when step k begins; step k's results (calculate_2D_CSR with wait=False)
+    are read back after step k+1 is enqueued."""
     import torch
-    csr = run.csr
-    main = torch.cuda.current_stream()
+    csr, beam = run.csr, run.beam
+    trk = csr.DF_tracker
+    last = first + count - 1
+    nb = len(dev_bufs)
+    copy = torch.cuda.Stream()
     h2d = d2h = 0
-    used = [None, None]           # event: last read of each device buffer (get_DF)
-    ready = [None, None]          # event: upload and moments of each buffer done
+    uploaded = {}                   # step -> event after its upload
 
-    def upload(k):
+    def upload(k, after=None):
         xpz = host_sets[k - 1]                      # pinned (3, N): x, px, z
-        buf = dev_bufs[k % 2]
-        with torch.cuda.stream(side):
-            if used[k % 2] is not None:
-                side.wait_event(used[k % 2])
+        buf = dev_bufs[k % nb]
+        with torch.cuda.stream(copy):
+            if after is not None:
+                copy.wait_event(after)              # the buffer's previous deposit
             buf[0].copy_(xpz[0], non_blocking=True)
             buf[1].copy_(xpz[1], non_blocking=True)
             buf[4].copy_(xpz[2], non_blocking=True)
+            uploaded[k] = copy.record_event()
         return xpz.numel() * 8
 
-    def moments(k):
-        run.beam.particle = dev_bufs[k % 2]
-        run.beam.update_status(stream=side, wait=False)
-        ready[k % 2] = side.record_event()
+    def status(k):
+        side.wait_event(uploaded.pop(k))
+        beam.particle = dev_bufs[k % nb]
+        return beam.status_async(side)
 
+    def deposit(k, st):
+        p = dev_bufs[k % nb]
+        return trk.deposit_DF(p[0], p[4], p[1], st.result(), side)
+
+    st = {}
+    for k in range(first, min(first + 1, last) + 1):
+        h2d += upload(k)
+        st[k] = status(k)
+    dep = {first: deposit(first, st[first])}
     pending = None
-    pre = None                    # step whose upload and moments are already enqueued
-    for k in range(first, first + count):
-        if pre != k:
-            h2d += upload(k)
-            moments(k)
-        run.beam.sync_status()
-        main.wait_event(ready[k % 2])
-        run.beam.position = float(run.plan.positions[k])
-        lf = run.plan.formation_length(k, run.beam.sigma_z)
-        csr.update_history(lf)
-        used[k % 2] = main.record_event()
+    for k in range(first, last + 1):
+        if k + 1 <= last:
+            dep[k + 1] = deposit(k + 1, st[k + 1])
+        if k + 2 <= last:
+            # buffer (k + 2) % 3 held step k - 1, whose deposit has been enqueued
+            prev = dep.get(k - 1)
+            h2d += upload(k + 2, prev.event if prev is not None else None)
+        beam.particle = dev_bufs[k % nb]
+        beam.apply_status(st.pop(k))
+        beam.position = float(run.plan.positions[k])
+        lf = run.plan.formation_length(k, beam.sigma_z)
+        d = dep.pop(k)
+        csr.update_history(lf, deposited=d)
+        dep[k - 1] = None
+        dep[k] = d                                  # kept until step k + 3's upload
         csr.get_CSR_mesh()
-        if k + 1 < first + count:
-            h2d += upload(k + 1)
         nxt = csr.calculate_2D_CSR(precision, wait=False)
-        if k + 1 < first + count:
-            moments(k + 1)
-            pre = k + 1
+        if k + 2 <= last:
+            st[k + 2] = status(k + 2)
         if pending is not None:
             dE, xk = pending.result()               # step k-1 on the host
             d2h += dE.nbytes + xk.nbytes
@@ -558,7 +571,7 @@ def gpu_arm(a):
             h = torch.empty((3, t.shape[1]), dtype=torch.float64, pin_memory=True)
             h.copy_(t[[0, 1, 4]])
             host_sets.append(h)
-        dev_bufs = [torch.zeros_like(sets[0]), torch.zeros_like(sets[0])]
+        dev_bufs = [torch.zeros_like(sets[0]) for _ in range(3)]
         e2e_steps(re2e, host_sets, 1, W, a.precision, dev_bufs, side)
         barrier()
         g0 = time.perf_counter()
