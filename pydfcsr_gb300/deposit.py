@@ -279,7 +279,9 @@ class DF_tracker:
         the current stream).  Returns a :class:`PendingDeposit` to hand to
         ``get_DF(..., deposited=...)``; the tracker's state is not touched,
         so the deposit of a later step can run while this step is finalised.
-        ``x``, ``z``, ``px`` must stay unchanged until the deposit has run."""
+        ``x``, ``z``, ``px`` must stay unchanged until the deposit has run.
+        Deposits of one tracker share its deposit scratch: two of them must
+        not be in flight on different streams at once."""
         require_cuda()
         st = np.asarray(moments, dtype=np.float64)
         s = stream if stream is not None else torch.cuda.current_stream()
