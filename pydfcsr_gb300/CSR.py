@@ -19,6 +19,9 @@ with the reference); ``'mixed'`` - FP32 bulk with the retarded geometry in
 double-word FP32 (~48 bits);
 ``'both'`` keeps both history rings so either can be called.
 """
+import datetime
+import os
+
 import numpy as np
 import torch
 
@@ -29,6 +32,12 @@ from .params import CSR_params, Integration_params
 from .runtime import as_device_f64, default_workspace, ptr, require_cuda, stream_handle
 
 __all__ = ["CSR2D", "WakeEvaluator", "PendingWake"]
+
+
+def _isotime():
+    """UTC time stamp for file names, local offset, ':' -> '_' (tools.py:16-22)."""
+    now = datetime.datetime.now(datetime.timezone.utc).astimezone().replace(microsecond=0)
+    return now.isoformat().replace(":", "_")
 
 
 def wake_job(tracker, lattice, position, sigma_z, sigma_x, slope0, mean_x, formation_length,
@@ -137,6 +146,7 @@ class CSR2D:
                 "lattice=, particle_deposition=, CSR_integration=, CSR_computation=")
         if precision not in ("fp64", "mixed", "both"):
             raise ValueError("precision must be 'fp64', 'mixed' or 'both'")
+        self.timestamp = _isotime()
         self.precision = precision
         self.near_band = float(near_band)
         self.beam = beam
@@ -383,3 +393,46 @@ class CSR2D:
                   1 if ignore_vx else 0, ptr(Iz), ptr(Ix), stream_handle())
         shape = np.shape(xp)
         return Iz.cpu().numpy().reshape(shape), Ix.cpu().numpy().reshape(shape)
+
+    # ------------------------------------------------------------- output
+    @property
+    def prefix(self):
+        """Output file prefix ``<write_name>-<timestamp>`` (CSR.py:41)."""
+        return f"{self.CSR_params.write_name}-{self.timestamp}"
+
+    def write_wakes(self):
+        """Append this step's wakes to ``<workdir>/<prefix>-wakes.h5``
+        (CSR.py:799-835), the layout ``postprocessor.py`` reads: group
+        ``step_<step>`` (attrs step, position, mean_gamma, beam_energy,
+        element, charge) with subgroups ``longitudinal`` (``x_grids``,
+        ``z_grids``, ``dE_dct``) and ``transverse`` (``x_grids``,
+        ``z_grids``, ``xkicks``), each with attr unit = 'MeV/m'; grids shaped
+        like the wake, [xbins, zbins].  Step 1 replaces an existing file.
+        Needs h5py; returns the file name."""
+        try:
+            import h5py
+        except ImportError as e:
+            raise ImportError("write_wakes writes HDF5 and needs h5py") from e
+        b = self.beam
+        filename = os.path.join(self.CSR_params.workdir, f"{self.prefix}-wakes.h5")
+        if b.step == 1 and os.path.isfile(filename):
+            os.remove(filename)
+        dE, xk = self.dE_dct, self.x_kick
+        x_grids = self.CSR_xmesh.reshape(dE.shape)
+        z_grids = self.CSR_zmesh.reshape(dE.shape)
+        element = getattr(self.lattice, "current_element", None)
+        with h5py.File(filename, "a") as hf:
+            g = hf.create_group(f"step_{b.step}")
+            g.attrs["step"] = b.step
+            g.attrs["position"] = b.position
+            g.attrs["mean_gamma"] = b.init_gamma
+            g.attrs["beam_energy"] = b.init_energy
+            g.attrs["element"] = "" if element is None else element
+            g.attrs["charge"] = b.charge
+            for name, wake, key in (("longitudinal", dE, "dE_dct"), ("transverse", xk, "xkicks")):
+                sub = g.create_group(name)
+                sub.attrs["unit"] = "MeV/m"
+                sub.create_dataset("x_grids", data=x_grids)
+                sub.create_dataset("z_grids", data=z_grids)
+                sub.create_dataset(key, data=wake)
+        return filename

@@ -12,6 +12,7 @@ one ``dfcsr_apply_wakes`` call.
 import ctypes
 
 import numpy as np
+import scipy.constants
 import torch
 
 from . import _lib
@@ -19,6 +20,9 @@ from .deposit import beam_moments
 from .runtime import as_device_f64, default_workspace, ptr, require_cuda, stream_handle
 
 __all__ = ["Beam"]
+
+# electron rest energy in eV, from scipy.constants (physical_constants.py:11)
+MC2 = scipy.constants.value("electron mass energy equivalent in MeV") * 1e6
 
 
 class PendingStatus:
@@ -174,6 +178,7 @@ class Beam:
     slope = property(lambda self: (self.sync_status(), self._slope.copy())[1])
     charge = property(lambda self: self._charge)
     init_energy = property(lambda self: self._init_energy)
+    init_gamma = property(lambda self: self._init_energy / MC2)
 
     @property
     def x_transform(self):
