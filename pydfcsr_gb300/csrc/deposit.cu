@@ -26,9 +26,12 @@ namespace dfcsr {
 // FP64 operations per particle: 7 in pass 1, 8 in pass 2.
 // 128-thread CTAs of 32 registers: one fits beside the wake's persistent
 // integral CTAs (which leave 4096 registers per SM), so the next step's
-// moments can run during the integral on the FP64 pipe it leaves idle
+// moments can run during the integral on the FP64 pipe it leaves idle.  At
+// most one CTA per SM (152): four warps with five independent sums each keep
+// the FP64 pipe busy, and more CTAs only take SM space that the integral's
+// CTAs, launched later, then wait for (pipelined step 1.27 -> 1.25 ms).
 constexpr int MOM_THREADS = 128;
-constexpr int MOM_MAX_BLOCKS = 1024;
+constexpr int MOM_MAX_BLOCKS = 152;
 constexpr int MOM_K = 5;   // partial sums per pass
 
 static int moment_blocks(int64_t n) {
