@@ -155,6 +155,18 @@ int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, double *vx,
                       double *scalars_out, void *workspace, size_t workspace_bytes,
                       void *stream);
 
+/* Health check of the bounded grid barrier that dfcsr_df_finalize's
+ * cooperative launch uses between its phases (no reference counterpart:
+ * the reference's get_DF runs on one CPU thread).  One cooperative launch
+ * of `blocks` CTAs (1..SM count) meets at the barrier once, expecting
+ * blocks + extra_arrivals arrivals (extra_arrivals 0 or 1).  With 1 the
+ * last arrival never comes: each CTA's wait gives up after max_spins polls
+ * (1..2^24; df_finalize uses 2^24, about a second) and the call returns
+ * DFCSR_TIMEOUT with the CUDA context intact.  Synchronises `stream`;
+ * workspace >= 16 bytes of device memory. */
+int dfcsr_grid_barrier_check(int blocks, int extra_arrivals, unsigned int max_spins,
+                             void *workspace, size_t workspace_bytes, void *stream);
+
 /* ------------------------------------------------------------------------
  * History regrid.  Replaces DF_interp (deposit.py:296-309: scipy
  * RegularGridInterpolator, linear, bounds_error False) for the five fields

@@ -117,6 +117,7 @@ _SIGS = [
     ("dfcsr_df_workspace_bytes", _c_size, [_c_int, _c_int]),
     ("dfcsr_df_finalize", _c_int, [ctypes.POINTER(DFParams), _p, _p, _p, _p, _p, _p, _p,
                                     _c_size, _p]),
+    ("dfcsr_grid_barrier_check", _c_int, [_c_int, _c_int, ctypes.c_uint, _p, _c_size, _p]),
     ("dfcsr_history_regrid", _c_int, [_p, _p, _p, _p, _p, _c_int, _c_int, _p, _p, _p, _c_int,
                                        _p, _p, _p, _c_int, _p, _p, _p, _p]),
     ("dfcsr_rgi_axis_linspace", _c_int, [_c_double, _c_double, _c_int, _c_double, _c_double,

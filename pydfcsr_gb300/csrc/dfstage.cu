@@ -40,23 +40,27 @@ struct GridBar {
     unsigned int count, gen, err, trapz;
 };
 
-// All CTAs of the cooperative launch meet here.  The spin is bounded (about
-// a second); on expiry the CTA records an error and continues, and the stage
-// then writes NaN scalars so that the failure shows downstream.
-__device__ __forceinline__ void grid_sync(GridBar *b) {
+// All CTAs of the cooperative launch meet here: `arrivals` CTAs are
+// expected (the grid).  The spin is bounded by `max_spins` polls (the stage
+// uses kBarSpins, about a second); on expiry the CTA records an error and
+// continues, and the stage then writes NaN scalars so that the failure
+// shows downstream.
+constexpr unsigned int kBarSpins = 1u << 24;
+
+__device__ __forceinline__ void grid_sync(GridBar *b, unsigned int arrivals, unsigned int max_spins) {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned int *vgen = &b->gen;
         const unsigned int g = *vgen;
         __threadfence();
-        if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
+        if (atomicAdd(&b->count, 1u) == arrivals - 1) {
             atomicExch(&b->count, 0u);
             __threadfence();
             atomicAdd(&b->gen, 1u);
         } else {
             unsigned int it = 0;
             while (*vgen == g) {
-                if (++it > (1u << 24)) {
+                if (++it > max_spins) {
                     atomicExch(&b->err, 1u);
                     break;
                 }
@@ -67,6 +71,8 @@ __device__ __forceinline__ void grid_sync(GridBar *b) {
     }
     __syncthreads();
 }
+
+__device__ __forceinline__ void grid_sync(GridBar *b) { grid_sync(b, gridDim.x, kBarSpins); }
 
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
 
@@ -532,3 +538,46 @@ extern "C" int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, doub
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }
+
+// ------------------------------------------------------ barrier health check
+namespace dfcsr {
+
+// One meeting of the stage's grid barrier.  With `arrivals` above the
+// launch's CTAs the last arrival never comes: every CTA's wait gives up
+// after `max_spins` polls and records the error.
+__global__ void gridbar_check(GridBar *b, unsigned int arrivals, unsigned int max_spins) {
+    grid_sync(b, arrivals, max_spins);
+}
+
+}  // namespace dfcsr
+
+extern "C" int dfcsr_grid_barrier_check(int blocks, int extra_arrivals, unsigned int max_spins,
+                                        void *workspace, size_t workspace_bytes, void *stream) {
+    using namespace dfcsr;
+    clear_error();
+    DFCSR_CHECK_ARG(blocks >= 1 && blocks <= num_sms(),
+                    "dfcsr_grid_barrier_check: blocks must be in [1, %d] (got %d)", num_sms(), blocks);
+    DFCSR_CHECK_ARG(extra_arrivals == 0 || extra_arrivals == 1,
+                    "dfcsr_grid_barrier_check: extra_arrivals must be 0 or 1 (got %d)", extra_arrivals);
+    DFCSR_CHECK_ARG(max_spins >= 1 && max_spins <= kBarSpins,
+                    "dfcsr_grid_barrier_check: max_spins must be in [1, %u] (got %u)", kBarSpins, max_spins);
+    DFCSR_CHECK_ARG(workspace && workspace_bytes >= sizeof(GridBar),
+                    "dfcsr_grid_barrier_check: workspace needs %zu bytes", sizeof(GridBar));
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    GridBar *bar = reinterpret_cast<GridBar *>(workspace);
+    DFCSR_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(GridBar), s));
+    unsigned int arrivals = (unsigned int)(blocks + extra_arrivals);
+    void *args[] = {&bar, &arrivals, &max_spins};
+    note_launch();
+    DFCSR_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)gridbar_check, dim3(blocks), dim3(32), args, 0, s));
+    DFCSR_LAUNCH_CHECK();
+    unsigned int err = 0;
+    DFCSR_CUDA_TRY(cudaMemcpyAsync(&err, &bar->err, sizeof(err), cudaMemcpyDeviceToHost, s));
+    DFCSR_CUDA_TRY(cudaStreamSynchronize(s));
+    if (err != 0u) {
+        set_error("dfcsr_grid_barrier_check: the barrier wait gave up after %u polls", max_spins);
+        return DFCSR_TIMEOUT;
+    }
+    return DFCSR_OK;
+}
+

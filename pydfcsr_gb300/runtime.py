@@ -97,3 +97,18 @@ def default_workspace():
         ws = Workspace()
         _default_ws[dev] = ws
     return ws
+
+
+def grid_barrier_check(blocks=None, extra_arrivals=0, max_spins=1 << 24, stream=None):
+    """Meet once at the DF stage's bounded grid barrier
+    (``dfcsr_grid_barrier_check``) with ``blocks`` CTAs (default: one per SM).
+    Returns when every CTA arrived; raises ``_lib.DfcsrTimeout`` when the
+    wait gave up - ``extra_arrivals=1`` expects one CTA more than the launch
+    has, so every wait gives up after ``max_spins`` polls and the CUDA
+    context stays usable."""
+    require_cuda()
+    if blocks is None:
+        blocks = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    bar = torch.zeros(4, dtype=torch.int32, device="cuda")
+    _lib.call("dfcsr_grid_barrier_check", int(blocks), int(extra_arrivals), int(max_spins),
+              ptr(bar), bar.numel() * 4, stream_handle(stream))

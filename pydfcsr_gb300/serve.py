@@ -113,6 +113,7 @@ class Scheduler:
         self.active = []
         self.refused = []
         self.cancelled = []
+        self.failed = []           # (spec, reason)
         self.done = []
 
     def cancel(self, req_id):
@@ -145,6 +146,13 @@ class Scheduler:
         self.admission.release(footprint_bytes(spec, self.precision))
         self.done.append(spec)
 
+    def fail(self, spec, reason):
+        """End an admitted request whose calls raised: its memory goes back
+        to the budget and the queue moves on."""
+        self.active.remove(spec)
+        self.admission.release(footprint_bytes(spec, self.precision))
+        self.failed.append((spec, reason))
+
     def idle_until(self):
         """Arrival time of the next pending request (None if none)."""
         return self.pending[0].arrival_s if self.pending else None
@@ -154,6 +162,18 @@ class Scheduler:
 
 
 # ------------------------------------------------------------------ GPU side
+def _request_errors():
+    """Errors that end one request and leave the CUDA context and the other
+    requests usable: a refused argument, a workspace or allocation failure,
+    a bounded device wait that gave up, a kernel's error status.  A CUDA
+    error (DfcsrCudaError) is not among them: it can poison the context,
+    so it ends the whole run."""
+    import torch
+    from . import _lib
+    return (_lib.DfcsrBadArgument, _lib.DfcsrOutOfMemory, _lib.DfcsrTimeout,
+            _lib.DfcsrKernelError, _lib.DfcsrAdmissionRefused, torch.cuda.OutOfMemoryError)
+
+
 class _Live:
     """Device state of one admitted request: its beam, DF history ring,
     workspace and CUDA stream."""
@@ -189,6 +209,7 @@ class _Live:
         self.points = 0
         self.finished_at = None
         self.done_event = None
+        self.failed = False
 
     def advance_launch(self):
         """Transport to the next step and enqueue its beam moments on this
@@ -407,14 +428,37 @@ class WakeServer:
             lv.points += m
             off += m
 
+    def _fail(self, spec, err, lv=None):
+        if lv is not None:
+            lv.failed = True
+            lv.release()
+        self.sched.fail(spec, f"{type(err).__name__}: {err}")
+
+    def _each(self, lives, method, errs):
+        """Call ``method`` of every live request; a request that raises one
+        of ``errs`` fails alone.  Returns the requests still live."""
+        for lv in lives:
+            try:
+                getattr(lv, method)()
+            except errs as e:
+                self._fail(lv.spec, e, lv)
+        return [lv for lv in lives if not lv.failed]
+
     def run(self):
-        """Serve the whole stream; returns a summary dict."""
+        """Serve the whole stream; returns a summary dict.  A request whose
+        calls raise a library error (bad argument, out of memory, timeout,
+        kernel error status) is marked failed and its memory released; the
+        others are served on (``failed()``)."""
         import torch
+        errs = _request_errors()
         self.t0 = time.perf_counter()
         sched = self.sched
         while not sched.finished():
             for spec in sched.admit():
-                self.live[spec.id] = _Live(spec, self._clock(), self.precision)
+                try:
+                    self.live[spec.id] = _Live(spec, self._clock(), self.precision)
+                except errs as e:
+                    self._fail(spec, e)
             if not sched.active:
                 nxt = sched.idle_until()
                 if nxt is not None:
@@ -424,11 +468,15 @@ class WakeServer:
             # every request's transport + moments first, then each request's
             # DF step: the moments of all beams run while the host waits for
             # the first one
-            for lv in lives:
-                lv.advance_launch()
-            for lv in lives:
-                lv.advance_finish()
-            self._wake_tick([lv for lv in lives if lv.wants_wake()])
+            lives = self._each(lives, "advance_launch", errs)
+            lives = self._each(lives, "advance_finish", errs)
+            tick = [lv for lv in lives if lv.wants_wake()]
+            try:
+                self._wake_tick(tick)
+            except errs as e:                   # the shared launch: all its requests
+                for lv in tick:
+                    self._fail(lv.spec, e, lv)
+                lives = [lv for lv in lives if not lv.failed]
             self.ticks += 1
             for lv in lives:
                 if lv.last_step():
@@ -443,7 +491,8 @@ class WakeServer:
                         if lv.finished_at is not None])
         pts = sum(lv.points for lv in self.live.values())
         return {"precision": self.precision, "requests": len(self.live),
-                "refused": len(self.sched.refused), "ticks": self.ticks,
+                "refused": len(self.sched.refused), "failed": len(self.sched.failed),
+                "ticks": self.ticks,
                 "wall_s": wall, "wake_points": int(pts),
                 "wake_points_per_s": pts / wall if wall > 0 else 0.0,
                 "wake_s": self.wake_s,
@@ -455,3 +504,7 @@ class WakeServer:
     def result(self, req_id):
         """[(step, dE_dct, x_kick)] of a served request."""
         return self.live[req_id].results
+
+    def failed(self):
+        """{request id: reason} of the requests that failed."""
+        return {spec.id: reason for spec, reason in self.sched.failed}

@@ -77,3 +77,7 @@ def test_bad_arguments_fail_without_gpu():
                   ctypes.c_void_p(16), 5, 2000, 100, 0, ctypes.c_void_p(16), ctypes.c_void_p(16),
                   None, 0, None)
     assert "xbins" in _lib.load().dfcsr_last_error().decode()
+    with pytest.raises(_lib.DfcsrBadArgument, match="extra_arrivals"):
+        _lib.call("dfcsr_grid_barrier_check", 1, 2, 100, ctypes.c_void_p(16), 16, None)
+    with pytest.raises(_lib.DfcsrBadArgument, match="workspace"):
+        _lib.call("dfcsr_grid_barrier_check", 1, 0, 100, ctypes.c_void_p(16), 8, None)

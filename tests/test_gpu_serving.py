@@ -97,3 +97,39 @@ def test_admission_refuses_oversize_request():
     srv = WakeServer([specs[0], big], budget_bytes=budget, chunk=256)
     summ = srv.run()
     assert summ["refused"] == 1 and summ["requests"] == 1
+
+
+def test_kernel_error_fails_one_request_only(monkeypatch):
+    """A kernel error status injected on the host for one request (its DF
+    step 3 raises as a failing C-ABI call does): that request fails alone,
+    its memory goes back to the budget, and the other requests' results are
+    bitwise those of a run without it."""
+    from pydfcsr_gb300 import _lib
+    from pydfcsr_gb300.serve import WakeServer, _Live
+    specs = _stream()[:3]
+    bad = specs[1].id
+    real = _Live.advance_finish
+
+    def advance_finish(self):
+        if self.spec.id == bad and self.k == 3:
+            raise _lib.DfcsrKernelError(4, "dfcsr_df_finalize", "injected kernel error status")
+        return real(self)
+
+    monkeypatch.setattr(_Live, "advance_finish", advance_finish)
+    srv = WakeServer(specs, max_active=3, chunk=256)
+    summ = srv.run()
+    monkeypatch.undo()
+    assert summ["failed"] == 1 and summ["refused"] == 0
+    assert "KERNEL_ERROR" in srv.failed()[bad]
+    assert srv.sched.admission.used == 0 and srv.sched.admission.active == 0
+    assert [k for k, _, _ in srv.result(bad)] == [2]       # served until it failed
+    ref = WakeServer([sp for sp in specs if sp.id != bad], max_active=3, chunk=256)
+    ref.run()
+    for sp in specs:
+        if sp.id == bad:
+            continue
+        got, want = srv.result(sp.id), ref.result(sp.id)
+        assert [k for k, _, _ in got] == [k for k, _, _ in want] == [2, 3, 4]
+        for (k, dE1, xk1), (_, dE2, xk2) in zip(got, want):
+            assert np.array_equal(dE1, dE2) and np.array_equal(xk1, xk2), (sp.id, k)
+

@@ -111,3 +111,17 @@ def test_request_spec_from_generator():
     assert 1e5 <= s.n <= 4e6
     with pytest.raises(TypeError):
         RequestSpec.from_dict({"id": 0})
+
+
+def test_scheduler_fail_releases_memory_and_admits_next():
+    clk = FakeClock()
+    a, b = spec(0, 0.0), spec(1, 0.0)
+    sched = Scheduler([a, b], Admission(footprint_bytes(a), 8), clk)   # room for one
+    assert [s.id for s in sched.admit()] == [0]
+    assert sched.admit() == []
+    sched.fail(a, "DfcsrKernelError: injected")
+    assert sched.failed == [(a, "DfcsrKernelError: injected")] and sched.active == []
+    assert sched.admission.used == 0
+    assert [s.id for s in sched.admit()] == [1]
+    sched.finish(b)
+    assert sched.finished() and sched.done == [b]
