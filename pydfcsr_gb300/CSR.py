@@ -394,6 +394,27 @@ class CSR2D:
         shape = np.shape(xp)
         return Iz.cpu().numpy().reshape(shape), Ix.cpu().numpy().reshape(shape)
 
+    # --------------------------------------------------------- checkpoint
+    def state_dict(self):
+        """(extension) The wake state between steps as host data: the DF
+        tracker's history (:meth:`DF_tracker.state_dict`), the formation
+        length, the CSR scaling and the output time stamp.  The beam's
+        particles are the caller's to save, as in the reference."""
+        return {"DF_tracker": self.DF_tracker.state_dict(),
+                "formation_length": self.formation_length,
+                "CSR_scaling": getattr(self, "CSR_scaling", None),
+                "timestamp": self.timestamp}
+
+    def load_state_dict(self, state):
+        """(extension) Resume from :meth:`state_dict` (same precision)."""
+        self.DF_tracker.load_state_dict(state["DF_tracker"])
+        self.formation_length = state["formation_length"]
+        if state["CSR_scaling"] is not None:
+            self.CSR_scaling = state["CSR_scaling"]
+        self.timestamp = state["timestamp"]
+        self._pending = None
+        self._jobs_dev = None
+
     # ------------------------------------------------------------- output
     @property
     def prefix(self):

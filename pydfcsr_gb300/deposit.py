@@ -469,6 +469,89 @@ class DF_tracker:
         self.delta_y = (self.max_y - self.min_y) / (self.x_grid_interp.shape[0] - 1)
         self.delta_z = (self.max_z - self.min_z) / (self.z_grid_interp.shape[0] - 1)
 
+    # -------------------------------------------------------- checkpoint
+    _STATE_SCALARS = ("sigma_x", "sigma_z", "xmean", "zmean", "start_time", "t", "end_time",
+                      "interp_start", "sigma_x_interp", "sigma_z_interp", "x_interp_lin",
+                      "z_interp_lin", "x_grids", "z_grids", "x_grid_interp", "z_grid_interp",
+                      "bins", "reinterpolated", "min_x", "max_x", "min_y", "max_y", "min_z",
+                      "max_z", "delta_x", "delta_y", "delta_z")
+    _STATE_LOGS = ("slope_log", "sigma_x_log", "sigma_z_log", "time_log", "time_interp")
+
+    def state_dict(self):
+        """(extension) The tracker's state as host data (numpy arrays, floats,
+        tuples; picklable): configuration, logs, every logged DF (fields and
+        finalisation scalars) and the history ring's slices in time order.
+        Waits for the device.  :meth:`load_state_dict` on a tracker of the
+        same precision resumes it: the steps that follow give the same
+        results bit for bit.  (The reference keeps its history in memory
+        only; its particle dumps, CSR.py:784-797, hold the beam.)"""
+        torch.cuda.synchronize()
+
+        def entry(e):
+            return {"x_grids": e.x_grids, "z_grids": e.z_grids, "x_lin": e.x_lin,
+                    "z_lin": e.z_lin, "fields": e.fields.cpu().numpy(),
+                    "scalars": e.scalars.cpu().numpy(), "t": e.t, "sigma_x": e.sigma_x,
+                    "sigma_z": e.sigma_z}
+
+        log = list(self.DF_log)
+        cur = next((i for i, e in enumerate(log) if e is self._cur), None)
+        ring = None
+        if self.ring is not None:
+            r = self.ring
+            idx = [(r.head + k) % r.cap for k in range(r.count)]
+            ring = {"nx": r.nx, "nz": r.nz, "count": r.count,
+                    "ring64": r.ring64[idx].cpu().numpy() if r.ring64 is not None else None,
+                    "ring32": r.ring32[idx].cpu().numpy() if r.ring32 is not None else None}
+        return {
+            "precision": self.precision, "grid_rule": self.grid_rule,
+            "config": {k: getattr(self, k) for k in ("xbins", "zbins", "xlim", "zlim",
+                                                     "filter_order", "filter_window",
+                                                     "velocity_threhold", "upper_limit")},
+            "scalars": {k: getattr(self, k) for k in self._STATE_SCALARS if hasattr(self, k)},
+            "stats": None if self.stats is None else np.array(self.stats, dtype=np.float64),
+            "logs": {k: list(getattr(self, k)) for k in self._STATE_LOGS},
+            "DF_log": [entry(e) for e in log],
+            "cur": cur if cur is not None else (None if self._cur is None else entry(self._cur)),
+            "ring": ring,
+        }
+
+    def load_state_dict(self, state):
+        """(extension) Restore a :meth:`state_dict` onto the current device."""
+        require_cuda()
+        if state["precision"] != self.precision:
+            raise ValueError(f"state of a '{state['precision']}' tracker, this one is "
+                             f"'{self.precision}'")
+        self.configure_params(**state["config"])
+        self.grid_rule = state["grid_rule"]
+        for k, v in state["scalars"].items():
+            setattr(self, k, v)
+        self.stats = None if state["stats"] is None else np.array(state["stats"])
+        for k in self._STATE_LOGS:
+            setattr(self, k, deque(state["logs"][k]))
+        dev = torch.device("cuda", torch.cuda.current_device())
+
+        def entry(e):
+            return _DFEntry(e["x_grids"], e["z_grids"], torch.from_numpy(e["fields"]).to(dev),
+                            torch.from_numpy(e["scalars"]).to(dev), e["t"], e["sigma_x"],
+                            e["sigma_z"], tuple(e["x_lin"]), tuple(e["z_lin"]))
+
+        self.DF_log = deque(entry(e) for e in state["DF_log"])
+        cur = state["cur"]
+        self._cur = self.DF_log[cur] if isinstance(cur, int) else (None if cur is None else entry(cur))
+        r = state["ring"]
+        self.ring = None
+        if r is not None:
+            ring = HistoryRing(r["nx"], r["nz"], r["ring64"] is not None, r["ring32"] is not None,
+                               cap=max(8, r["count"] + 4), device=dev)
+            for k in range(r["count"]):
+                s64, s32 = ring.push()
+                if s64 is not None:
+                    s64.copy_(torch.from_numpy(r["ring64"][k]))
+                if s32 is not None:
+                    s32.copy_(torch.from_numpy(r["ring32"][k]))
+            self.ring = ring
+        torch.cuda.synchronize()
+
     # stacked host copies, like the reference's data_*_interp arrays
     data_density_interp = property(lambda self: self.ring.stacked("density"))
     data_density_x_interp = property(lambda self: self.ring.stacked("density_x"))
