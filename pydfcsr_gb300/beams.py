@@ -50,6 +50,28 @@ class Beam:
         self.step = 0
         self.set_coords(coords, adopt)
 
+    @classmethod
+    def from_particle(cls, particle, charge=1e-9, **kw):
+        """A beam from a bmadx-style ``Particle`` (fields x..pz, s, p0c; numpy
+        or torch arrays), as the reference's Beam holds one (beams.py:33):
+        energy = p0c, position = s."""
+        coords = [getattr(particle, k) for k in ("x", "px", "y", "py", "z", "pz")]
+        if isinstance(coords[0], torch.Tensor):
+            coords = torch.stack([c.to(torch.float64) for c in coords])
+        else:
+            coords = np.stack([np.asarray(c, dtype=np.float64) for c in coords])
+        return cls(coords, charge=charge, energy=float(particle.p0c), position=float(particle.s),
+                   **kw)
+
+    def to_particle(self):
+        """The particles as a bmadx-style ``Particle`` of host numpy arrays
+        (s = position, p0c = the initial energy, mc2 = the electron's), for
+        :func:`pydfcsr_gb300.interfaces.bmadx_particles_to_openpmd`."""
+        from .interfaces import M_ELECTRON, Particle
+        h = self.particle.cpu().numpy()
+        return Particle(*[h[k].copy() for k in range(6)], s=self.position,
+                        p0c=self._init_energy, mc2=M_ELECTRON)
+
     def set_coords(self, coords, adopt=False):
         """Replace the particle coordinates (array-like [6, N]).
 

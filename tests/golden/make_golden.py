@@ -357,8 +357,41 @@ def gen_apply_wakes(R):
     save("apply_wakes.npz", **out)
 
 
+def gen_interfaces(R):
+    """interfaces.py:13-127 on a small beam: openPMD -> bmadx coordinates,
+    and bmadx -> openPMD data from numpy and from torch particles.  The
+    shim's bmadx Particle and ParticleGroup are replaced by a namedtuple and
+    a function returning the data dict, so the reference's arithmetic is
+    recorded as is."""
+    import collections
+    import types
+    import torch
+    import pyDFCSR_2D.interfaces as I
+    Part = collections.namedtuple("Particle", "x px y py z pz s p0c mc2")
+    I.Particle = Part
+    I.ParticleGroup = lambda data: data
+    rng = np.random.default_rng(46)
+    n, p0c = 128, 1.0e9
+    pmd = types.SimpleNamespace(x=rng.normal(0, 2e-5, n), px=rng.normal(0, 5e3, n),
+                                y=rng.normal(0, 1e-5, n), py=rng.normal(0, 3e3, n),
+                                z=rng.normal(0, 5e-5, n), p=p0c * (1 + rng.normal(0, 1e-3, n)))
+    coords = np.array(I.openpmd_to_bmadx_coords(pmd, p0c))
+    part = I.openpmd_to_bmadx_particles(pmd, p0c, s=0.37)
+    out = {"x": pmd.x, "px": pmd.px, "y": pmd.y, "py": pmd.py, "z": pmd.z, "p": pmd.p,
+           "p0c": np.array(p0c), "s": np.array(0.37), "charge": np.array(1e-9),
+           "coords": coords, "mc2": np.array(part.mc2)}
+    keys = ("x", "px", "y", "py", "z", "pz", "t", "weight")
+    dat = I.bmadx_particles_to_openpmd(part, 1e-9)
+    out["pmd_numpy"] = np.array([dat[k] for k in keys])
+    tpart = Part(*[torch.from_numpy(c.copy()) for c in coords], 0.37, p0c, part.mc2)
+    dat = I.bmadx_particles_to_openpmd(tpart, 1e-9)
+    out["pmd_torch"] = np.array([dat[k] for k in keys])
+    save("interfaces.npz", **out)
+
+
 def main(ref_root):
     R = ref_shim.install(ref_root)
+    gen_interfaces(R)
     gen_apply_wakes(R)
     gen_interp(R)
     gen_cic(R)

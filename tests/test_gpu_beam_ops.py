@@ -122,3 +122,23 @@ def test_transport_strided_rows():
     ref = R @ full[:, :700]
     assert np.abs(out[:, :700] - ref).max() <= 1e-14 * np.abs(ref).max()
     np.testing.assert_array_equal(out[:, 700:], full[:, 700:])
+
+
+def test_beam_from_and_to_particle():
+    """Beam.from_particle / to_particle: a bmadx-style Particle (numpy or
+    torch arrays) in, the same coordinates, energy and position out, ready
+    for interfaces.bmadx_particles_to_openpmd."""
+    torch = _torch()
+    from pydfcsr_gb300 import interfaces as I
+    from pydfcsr_gb300.beams import Beam
+    rng = np.random.default_rng(9)
+    c = rng.normal(0, 1e-4, (6, 1000))
+    for arrays in ([r.copy() for r in c], [torch.from_numpy(r.copy()) for r in c]):
+        part = I.Particle(*arrays, s=0.25, p0c=1.2e9, mc2=I.M_ELECTRON)
+        beam = Beam.from_particle(part, charge=2e-9)
+        assert beam.position == 0.25 and beam.init_energy == 1.2e9 and beam.charge == 2e-9
+        back = beam.to_particle()
+        assert np.array_equal(np.array(back[:6]), c)
+        assert back.s == 0.25 and back.p0c == 1.2e9 and back.mc2 == I.M_ELECTRON
+        dat = I.bmadx_particles_to_openpmd(back, 2e-9)
+        assert np.allclose(dat["weight"].sum(), 2e-9)
