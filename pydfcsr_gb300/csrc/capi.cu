@@ -23,10 +23,13 @@ static std::atomic<long long> g_launches{0};
 
 void note_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
+// SM count of the current device; without one (argument checks on a host
+// with no GPU) that of a GB300
 int num_sms() {
+    constexpr int kGb300Sms = 152;
     int dev = 0, n = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 148;
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 148;
+    if (cudaGetDevice(&dev) != cudaSuccess) return kGb300Sms;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return kGb300Sms;
     return n;
 }
 
