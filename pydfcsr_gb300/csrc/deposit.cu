@@ -7,8 +7,9 @@
 // cell into four moments per weight channel (sum w, w f1, w f2, w f1 f2 of
 // the fractional offsets), and a gather pass forms the four corner sums that
 // land on each output cell.  Same result for the same input on every run; no
-// floating-point atomics anywhere.  GB300 runs FP64 at 1/64 of the FP32 rate,
-// so the per-particle FP64 work is kept to 6 (keys) + 10 (sums) operations.
+// floating-point atomics anywhere.  GB300 runs FP64 at about 1/72 of the
+// FP32 rate (measured FMA rates), so the per-particle FP64 work is kept to
+// 6 (keys) + 10 (sums) operations.
 #include "dfcsr_common.cuh"
 
 namespace dfcsr {
