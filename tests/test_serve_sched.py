@@ -125,3 +125,15 @@ def test_scheduler_fail_releases_memory_and_admits_next():
     assert [s.id for s in sched.admit()] == [1]
     sched.finish(b)
     assert sched.finished() and sched.done == [b]
+
+
+def test_request_errors_leave_cuda_errors_fatal():
+    """A library error ends one request; a CUDA error (which can poison the
+    context) is not among the per-request errors, so it ends the run."""
+    from pydfcsr_gb300 import _lib
+    from pydfcsr_gb300.serve import _request_errors
+    errs = _request_errors()
+    for cls in (_lib.DfcsrBadArgument, _lib.DfcsrOutOfMemory, _lib.DfcsrTimeout,
+                _lib.DfcsrKernelError, _lib.DfcsrAdmissionRefused):
+        assert issubclass(cls, errs)
+    assert not issubclass(_lib.DfcsrCudaError, errs)

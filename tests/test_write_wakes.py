@@ -117,3 +117,17 @@ def test_write_wakes_needs_h5py(tmp_path, monkeypatch):
     monkeypatch.setitem(sys.modules, "h5py", None)
     with pytest.raises(ImportError, match="h5py"):
         _csr(tmp_path, 1).write_wakes()
+
+
+def test_prefix_and_timestamp_format():
+    """<write_name>-<ISO time, ':' replaced by '_'> as the reference's
+    isotime (tools.py:16-22) and CSR2D.prefix (CSR.py:41)."""
+    import re
+    from pydfcsr_gb300.CSR import _isotime
+    ts = _isotime()
+    assert ":" not in ts
+    assert re.fullmatch(r"\d{4}-\d\d-\d\dT\d\d_\d\d_\d\d[+-]\d\d_\d\d", ts)
+    csr = object.__new__(CSR2D)
+    csr.CSR_params = CSR_params({"write_name": "run7"})
+    csr.timestamp = ts
+    assert csr.prefix == f"run7-{ts}"
