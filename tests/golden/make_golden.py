@@ -1,8 +1,10 @@
 """Generate the golden fixtures of the wake path by running the reference itself.
 
-Run in a container that holds the pyDFCSR_2D source tree (read-only is fine):
+Run in a container that holds the pyDFCSR_2D source tree (read-only is fine),
+giving the directory that contains ``pyDFCSR_2D/``; optional fixture names
+after it regenerate only those fixtures:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout> [r_gen6 ...]
 
 The reference is imported through ``ref_shim`` (stub modules for numba,
 bmadx, h5py, mpi4py, yaml, distgen, pmd_beamphysics and matplotlib; numba
@@ -26,6 +28,10 @@ Fixtures:
                 calculate_2D_CSR for an unchirped dipole and for both signs of
                 chirp (the 4-region branch).
   apply_wakes.npz  Beam.apply_wakes with and without the transverse kick.
+  r_gen6.npz    r_gen6 matrices (drift, sector and rectangular bends with
+                edges and half gap, quadrupoles of both signs, combined
+                function, rolls, the pure rotation) and the three tracked
+                vectors of the reference's BmadX tracking notebook.
 """
 import os
 import sys
@@ -389,15 +395,36 @@ def gen_interfaces(R):
     save("interfaces.npz", **out)
 
 
-def main(ref_root):
-    R = ref_shim.install(ref_root)
-    gen_interfaces(R)
-    gen_apply_wakes(R)
-    gen_interp(R)
-    gen_cic(R)
-    gen_df(R)
-    gen_lattice(R)
-    gen_history(R)
+R_GEN6_CASES = [
+    # (L, angle, k1, roll, E1, E2, hgap)
+    (1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0),           # drift (notebook)
+    (0.1, 0.05, 0.0, 0.0, 0.0, 0.1, 0.0),          # sbend with exit edge (notebook)
+    (0.1, 0.0, 10.0, 0.0, 0.0, 0.0, 0.0),          # focusing quad (notebook)
+    (0.2, 0.0, -7.5, 0.0, 0.0, 0.0, 0.0),          # defocusing quad
+    (0.5, 0.05, 0.0, 0.0, 0.0, 0.0, 0.0),          # chicane sector bend
+    (0.5, -0.05, 0.0, 0.0, 0.0, 0.0, 0.0),
+    (0.3, 0.2, 0.0, 0.0, 0.1, 0.1, 0.0),           # rectangular bend
+    (0.3, 0.2, 0.0, 0.0, 0.1, 0.1, 0.02),          # with fringe-field half gap
+    (0.4, 0.1, 1.5, 0.0, 0.0, 0.0, 0.0),           # combined function
+    (0.4, 0.1, -3.0, 0.3, 0.02, -0.03, 0.01),      # rolled combined function, edges
+    (0.2, 0.0, 5.0, np.pi / 4, 0.0, 0.0, 0.0),     # skew quad
+    (0.0, 0.0, 0.0, 0.7, 0.0, 0.0, 0.0),           # pure rotation
+    (0.25, 1e-13, 0.0, 0.0, 0.0, 0.0, 0.0),        # almost no bend
+]
+
+
+def gen_r_gen6(R):
+    """r_gen6 (r_gen6.py:4-122) on the cases above, and R @ (1e-3 * ones(6))
+    for the notebook's three elements (test/test_BmadX_tracking.ipynb)."""
+    cases = np.array(R_GEN6_CASES, dtype=np.float64)
+    mats = np.array([R.r_gen6.r_gen6(L=c[0], angle=c[1], k1=c[2], roll=c[3], E1=c[4], E2=c[5],
+                                     hgap=c[6]) for c in cases])
+    coords = np.ones(6) * 1e-3
+    tracked = np.array([np.matmul(mats[k], coords) for k in range(3)])
+    save("r_gen6.npz", cases=cases, mats=mats, tracked=tracked)
+
+
+def gen_wakes(R):
     dep = {"xbins": 40, "zbins": 48, "xlim": 5, "zlim": 5, "filter_order": 2,
            "filter_window": 5, "velocity_threhold": 1000, "upper_limit": 36}
     integ = {"n_formation_length": 1.5, "zbins": 16, "xbins": 12}
@@ -422,5 +449,22 @@ def main(ref_root):
              full_mesh=False)
 
 
+GENERATORS = {"interfaces": gen_interfaces, "apply_wakes": gen_apply_wakes, "interp": gen_interp,
+              "cic": gen_cic, "df": gen_df, "lattice": gen_lattice, "history": gen_history,
+              "wake": gen_wakes, "r_gen6": gen_r_gen6}
+
+
+def main(ref_root, only=None):
+    R = ref_shim.install(ref_root)
+    want = list(only or GENERATORS)
+    bad = [w for w in want if w not in GENERATORS]
+    if bad:
+        raise SystemExit(f"unknown fixtures {bad}; choose from {sorted(GENERATORS)}")
+    for name in want:
+        GENERATORS[name](R)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: make_golden.py <directory holding pyDFCSR_2D/> [fixture ...]")
+    main(sys.argv[1], sys.argv[2:] or None)
