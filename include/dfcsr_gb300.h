@@ -108,10 +108,14 @@ int dfcsr_deposit_cic2d(const double *q1, const double *q2, const double *w0,
  * every GPU that loads this entry point, held until exit).  Same arguments
  * and results as dfcsr_deposit_cic2d without the workspace.  Limits: at most
  * 1,048,576 particles and (nb1 + 1) * (nb2 + 1) <= 257 * 257 (a 256 x 256
- * grid); larger requests return DFCSR_BAD_ARG.  The first call on a device
- * resolves the array's device address (cudaGetSymbolAddress) and should come
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race and must be serialised by the caller. */
+ * grid); larger requests return DFCSR_BAD_ARG.  A call resolves the array's
+ * device address (cudaGetSymbolAddress) on the current device, again on every
+ * call made outside a stream capture (an address from before a
+ * cudaDeviceReset would be stale); a call on a capturing stream uses the
+ * address of the device's last call outside a capture, so the first call on
+ * a device must come before any stream capture (else DFCSR_BAD_ARG).  All
+ * calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
 size_t dfcsr_deposit_noalloc_max_bytes(void);
 int dfcsr_deposit_cic2d_noalloc(const double *q1, const double *q2, const double *w0,
                                 const double *w1, int64_t n,
@@ -141,12 +145,20 @@ typedef struct {
     const double *dzg;          /* [nz-1] diff(z_grids)                       */
     int gx_uniform, gz_uniform; /* numpy.gradient uniform-spacing path taken  */
     double gx_dx, gz_dx;        /* the uniform spacing when taken             */
+    unsigned int barrier_spins; /* polls before a grid-barrier wait gives up  */
+                                /* (0: 2^24, about a second; at most 2^24)    */
+    int barrier_extra;          /* 0; 1 expects one arrival more than the     */
+                                /* launch has CTAs, so that every wait runs   */
+                                /* out (exercises the timeout path)           */
 } dfcsr_df_params;
 
 /* density, vx: in = raw deposits, out = final fields.  density_x,
  * density_z, vx_x: outputs.  scalars_out[8] (device): 0 dsum, 1 thr,
- * 2 thr2, 3 vx_x fill, 4 mean(vx_x), 5 max raw density, 6 max density
- * (all NaN if a grid barrier of the launch timed out).  nz <= 16384.
+ * 2 thr2, 3 vx_x fill, 4 mean(vx_x), 5 max raw density, 6 max density,
+ * 7 status: 0.0, or 1.0 if a grid-barrier wait of the launch gave up - the
+ * fields are then invalid and scalars 0..6 are NaN.  The call returns before
+ * the launch ends, so the caller reads scalars_out[7] once the stream has
+ * passed it (DF_tracker raises DfcsrTimeout from it).  nz <= 16384.
  * One cooperative launch (one CTA per SM, all resident) on `stream`.
  * Scratch: dfcsr_df_workspace_bytes(nx, nz). */
 size_t dfcsr_df_workspace_bytes(int nx, int nz);

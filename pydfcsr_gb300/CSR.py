@@ -26,7 +26,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .deposit import DF_tracker
+from .deposit import DF_tracker, raise_if_df_failed
 from .lattice import Lattice
 from .params import CSR_params, Integration_params
 from .runtime import as_device_f64, default_workspace, ptr, require_cuda, stream_handle
@@ -113,13 +113,22 @@ class WakeEvaluator:
 
 class PendingWake:
     """Mesh wake whose device->host copy is in flight: ``result()`` waits for
-    it and returns (dE_dct, x_kick) as numpy arrays of ``shape``."""
+    it and returns (dE_dct, x_kick) as numpy arrays of ``shape``.
 
-    def __init__(self, dE, xk, shape):
+    ``status``: DF finalisations whose status words travel with the copy
+    (``DF_tracker.take_unchecked()``); ``result()`` raises DfcsrTimeout if one
+    of them reports a grid-barrier wait that gave up."""
+
+    def __init__(self, dE, xk, shape, status=()):
         n = dE.numel()
+        cur = torch.cuda.current_stream()
         self._host = torch.empty((2, n), dtype=torch.float64, pin_memory=True)
         self._host[0].copy_(dE, non_blocking=True)
         self._host[1].copy_(xk, non_blocking=True)
+        self._flags = torch.zeros(len(status), dtype=torch.float64, pin_memory=True)
+        for k, (sc, ev) in enumerate(status):
+            cur.wait_event(ev)
+            self._flags[k:k + 1].copy_(sc[7:8], non_blocking=True)
         self._event = torch.cuda.Event()
         self._event.record()
         self.shape = shape
@@ -130,6 +139,7 @@ class PendingWake:
 
     def result(self):
         self._event.synchronize()
+        raise_if_df_failed(self._flags.numpy())
         h = self._host.numpy()
         return h[0].reshape(self.shape).copy(), h[1].reshape(self.shape).copy()
 
@@ -268,7 +278,9 @@ class CSR2D:
 
     def wake_device(self, s, x, precision=None, stream=None):
         """dE/dct and x-kick at device observation points (float64 CUDA
-        tensors) - the hot-path call."""
+        tensors) - the hot-path call.  Nothing is read back: a caller that
+        keeps the results on the device checks the DF finalisations with
+        ``DF_tracker.check_status()`` when it next synchronises."""
         kind = self._wake_kind(precision)
         jobs = jobs_to_device([self._job()])
         self._jobs_dev = jobs
@@ -284,11 +296,13 @@ class CSR2D:
 
         ``wait=False`` (extension) returns at once with a :class:`PendingWake`;
         the results are copied to pinned host memory on the stream and
-        ``dE_dct`` / ``x_kick`` wait for that copy when first read."""
+        ``dE_dct`` / ``x_kick`` wait for that copy when first read.  Reading
+        the results raises DfcsrTimeout if a DF finalisation of the history
+        since the previous wake reported a barrier wait that gave up."""
         s, x = self.mesh_device()
         dE, xk = self.wake_device(s, x, precision)
         shape = (self.CSR_params.xbins, self.CSR_params.zbins)
-        pending = PendingWake(dE, xk, shape)
+        pending = PendingWake(dE, xk, shape, self.DF_tracker.take_unchecked())
         self._pending = pending
         if wait:
             self._resolve()

@@ -69,6 +69,7 @@ class DFParams(ctypes.Structure):
         ("dxg", _p), ("dzg", _p),
         ("gx_uniform", _c_int), ("gz_uniform", _c_int),
         ("gx_dx", _c_double), ("gz_dx", _c_double),
+        ("barrier_spins", ctypes.c_uint), ("barrier_extra", _c_int),
     ]
 
 

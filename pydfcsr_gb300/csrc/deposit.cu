@@ -624,6 +624,7 @@ extern "C" int dfcsr_beam_moments(const double *x, const double *z, int64_t n, d
 
 extern "C" size_t dfcsr_deposit_workspace_bytes(int64_t n, int nb1, int nb2) {
     if (n < 0 || nb1 <= 0 || nb2 <= 0) return 0;
+    if (((int64_t)nb1 + 1) * ((int64_t)nb2 + 1) >= (1ll << 30)) return 0;   // refused by the deposit
     const DepositLayout L = deposit_layout(n, nb1, nb2);
     Carver c{nullptr, 0, 0};
     uint32_t *a, *b, *cc, *d, *e, *f, *g, *h;
@@ -639,7 +640,7 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
     clear_error();
     DFCSR_CHECK_ARG(out0, "dfcsr_deposit_cic2d: out0 is null");
     DFCSR_CHECK_ARG(nb1 > 0 && nb2 > 0, "dfcsr_deposit_cic2d: bins must be positive (%d, %d)", nb1, nb2);
-    DFCSR_CHECK_ARG((int64_t)(nb1 + 1) * (nb2 + 1) < (1ll << 30),
+    DFCSR_CHECK_ARG(((int64_t)nb1 + 1) * ((int64_t)nb2 + 1) < (1ll << 30),
                     "dfcsr_deposit_cic2d: grid %d x %d too large", nb1, nb2);
     DFCSR_CHECK_ARG(n >= 0 && n < (1ll << 32) - 1, "dfcsr_deposit_cic2d: bad particle count %lld",
                     (long long)n);

@@ -31,17 +31,30 @@ static __device__ __align__(256) unsigned char g_deposit_scratch[kNoAllocScratch
 static std::mutex g_noalloc_mu;
 static void *g_noalloc_ptr[128];   // device address of g_deposit_scratch per device
 
-// Set-up, once per device with that device current: the host-side name of a
-// __device__ array is not a device address, so resolve the address first.
-static int noalloc_scratch(void **out) {
+// Set-up, with the calling device current: the host-side name of a
+// __device__ array is not a device address, so the address is resolved with
+// cudaGetSymbolAddress.  It is resolved again on every call made outside a
+// stream capture (after a cudaDeviceReset the module is loaded anew and an
+// address kept from before would be stale); a call made while `stream` is
+// being captured uses the address resolved by the device's last call outside
+// a capture, so the first call on a device must come before any capture.
+static int noalloc_scratch(cudaStream_t stream, void **out) {
     int dev = 0;
     DFCSR_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 128) {
         set_error("dfcsr_deposit_cic2d_noalloc: device ordinal %d out of range", dev);
         return DFCSR_BAD_ARG;
     }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    DFCSR_CUDA_TRY(cudaStreamIsCapturing(stream, &cap));
     std::lock_guard<std::mutex> g(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    if (cap != cudaStreamCaptureStatusNone) {
+        if (!g_noalloc_ptr[dev]) {
+            set_error("dfcsr_deposit_cic2d_noalloc: the first call on device %d must come before "
+                      "any stream capture", dev);
+            return DFCSR_BAD_ARG;
+        }
+    } else {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_deposit_scratch);
         if (e != cudaSuccess || !p) {
@@ -69,7 +82,7 @@ extern "C" int dfcsr_deposit_cic2d_noalloc(const double *q1, const double *q2, c
     DFCSR_CHECK_ARG(n >= 0 && n <= kNoAllocMaxParticles,
                     "dfcsr_deposit_cic2d_noalloc: %lld particles exceed the no-alloc maximum of "
                     "%lld", (long long)n, kNoAllocMaxParticles);
-    DFCSR_CHECK_ARG(nb1 > 0 && nb2 > 0 && (long long)(nb1 + 1) * (nb2 + 1) <= kNoAllocMaxKeys,
+    DFCSR_CHECK_ARG(nb1 > 0 && nb2 > 0 && ((long long)nb1 + 1) * ((long long)nb2 + 1) <= kNoAllocMaxKeys,
                     "dfcsr_deposit_cic2d_noalloc: grid %d x %d exceeds the no-alloc maximum "
                     "((nb1 + 1) * (nb2 + 1) <= %lld, i.e. 256 x 256)", nb1, nb2, kNoAllocMaxKeys);
     const size_t need = dfcsr_deposit_workspace_bytes(n, nb1, nb2);
@@ -77,7 +90,7 @@ extern "C" int dfcsr_deposit_cic2d_noalloc(const double *q1, const double *q2, c
                     "dfcsr_deposit_cic2d_noalloc: needs %zu bytes of scratch, more than the "
                     "%zu reserved", need, kNoAllocScratchBytes);
     void *scratch = nullptr;
-    const int st = noalloc_scratch(&scratch);
+    const int st = noalloc_scratch(as_stream(stream), &scratch);
     if (st != DFCSR_OK) return st;
     return dfcsr_deposit_cic2d(q1, q2, w0, w1, n, nb1, start1, end1, nb2, start2, end2, out0, out1,
                                scratch, kNoAllocScratchBytes, stream);

@@ -20,6 +20,8 @@
 // dependent steps (FP64 latency, barriers), so sums are trees, not chains.
 // Data written by other CTAs during the launch is read with ld.global.cg
 // (from L2), never through the non-coherent L1.
+#include <mutex>
+
 #include "dfcsr_common.cuh"
 
 namespace dfcsr {
@@ -43,28 +45,33 @@ struct GridBar {
 // All CTAs of the cooperative launch meet here: `arrivals` CTAs are
 // expected (the grid).  The spin is bounded by `max_spins` polls (the stage
 // uses kBarSpins, about a second); on expiry the CTA records an error and
-// continues, and the stage then writes NaN scalars so that the failure
-// shows downstream.
+// continues.  Once an error is recorded no CTA waits at a barrier again (the
+// arrival count is out of step after a wait gave up, so a later meeting
+// could release early or never): every CTA runs to the end of the launch,
+// and the stage then writes NaN scalars and its error flag.
 constexpr unsigned int kBarSpins = 1u << 24;
 
 __device__ __forceinline__ void grid_sync(GridBar *b, unsigned int arrivals, unsigned int max_spins) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned int *vgen = &b->gen;
-        const unsigned int g = *vgen;
-        __threadfence();
-        if (atomicAdd(&b->count, 1u) == arrivals - 1) {
-            atomicExch(&b->count, 0u);
+        volatile unsigned int *verr = &b->err;
+        if (*verr == 0u) {
+            volatile unsigned int *vgen = &b->gen;
+            const unsigned int g = *vgen;
             __threadfence();
-            atomicAdd(&b->gen, 1u);
-        } else {
-            unsigned int it = 0;
-            while (*vgen == g) {
-                if (++it > max_spins) {
-                    atomicExch(&b->err, 1u);
-                    break;
+            if (atomicAdd(&b->count, 1u) == arrivals - 1) {
+                atomicExch(&b->count, 0u);
+                __threadfence();
+                atomicAdd(&b->gen, 1u);
+            } else {
+                unsigned int it = 0;
+                while (*vgen == g && *verr == 0u) {
+                    if (++it > max_spins) {
+                        atomicExch(&b->err, 1u);
+                        break;
+                    }
+                    __nanosleep(64);
                 }
-                __nanosleep(64);
             }
         }
         __threadfence();
@@ -72,7 +79,12 @@ __device__ __forceinline__ void grid_sync(GridBar *b, unsigned int arrivals, uns
     __syncthreads();
 }
 
-__device__ __forceinline__ void grid_sync(GridBar *b) { grid_sync(b, gridDim.x, kBarSpins); }
+// The stage's barrier: the grid's CTAs plus p.barrier_extra (0; 1 only to
+// exercise the timeout path: an arrival that never comes), at most
+// p.barrier_spins polls (0: kBarSpins).
+__device__ __forceinline__ void grid_sync(GridBar *b, const dfcsr_df_params &p) {
+    grid_sync(b, gridDim.x + (unsigned int)p.barrier_extra, p.barrier_spins ? p.barrier_spins : kBarSpins);
+}
 
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
 
@@ -286,7 +298,7 @@ df_stage(DfArgs A) {
 
     // max of the raw density (deposit.py:183)
     reduce_part<0>(A.density, nullptr, n, 0.0, A.part0, red);
-    grid_sync(A.bar);
+    grid_sync(A.bar, p);
     // thr = max / vth (every CTA combines the partials); smoothing along x of
     // density and of vx / density where density > thr (deposit.py:183-195)
     {
@@ -298,14 +310,14 @@ df_stage(DfArgs A) {
         sg_phase<0>(LoadThrDiv{A.density, A.vx, thr, nz}, dst, 2, nx, nz, w, p.sg_coeff, p.sg_lo,
                     p.sg_hi, tile);
     }
-    grid_sync(A.bar);
+    grid_sync(A.bar, p);
     // ... then along z, into density and vx
     {
         double *dst[2] = {A.density, A.vx};
         sg_phase<1>(LoadPlain<1>{{A.T0, A.T1, nullptr}, nz}, dst, 2, nx, nz, w, p.sg_coeff, p.sg_lo,
                     p.sg_hi, tile);
     }
-    grid_sync(A.bar);
+    grid_sync(A.bar, p);
     // trapz (deposit.py:197-199): col[j] = sum over rows i of
     // (dx_i * (d[i+1][j] + d[i][j])) / 2.0 by a fixed tree.  Virtual block =
     // 32 columns x TRAPZ_ROWS rows: warp w adds its 4 rows as a pair of
@@ -366,7 +378,7 @@ df_stage(DfArgs A) {
             }
         }
     }
-    grid_sync(A.bar);
+    grid_sync(A.bar, p);
     // density /= dsum; vx[density <= thr] = 0 (deposit.py:201-204), and the
     // max of the normalised density (deposit.py:229) over the reduction's
     // element assignment
@@ -388,7 +400,7 @@ df_stage(DfArgs A) {
             }
         }
     }
-    grid_sync(A.bar);
+    grid_sync(A.bar, p);
     // gradients (deposit.py:207-215), formed while staging, smoothed along x ...
     {
         double *dst[3] = {A.T0, A.T1, A.T2};
@@ -396,21 +408,21 @@ df_stage(DfArgs A) {
                              p.gz_dx},
                     dst, 3, nx, nz, w, p.sg_coeff, p.sg_lo, p.sg_hi, tile);
     }
-    grid_sync(A.bar);
+    grid_sync(A.bar, p);
     // ... and along z into density_x, density_z, vx_x
     {
         double *dst[3] = {A.density_x, A.density_z, A.vx_x};
         sg_phase<1>(LoadPlain<1>{{A.T0, A.T1, A.T2}, nz}, dst, 3, nx, nz, w, p.sg_coeff, p.sg_lo, p.sg_hi,
                     tile);
     }
-    grid_sync(A.bar);
+    grid_sync(A.bar, p);
     // thr2 = max(density) / vth * 8; mean of vx_x over density > thr2
     // (deposit.py:229-231)
     double mx2, c2;
     reduce_combine<0>(A.part1, tile, mx2, c2);
     const double thr2 = __dmul_rn(__ddiv_rn(mx2, vth), 8.0);
     reduce_part<1>(A.density, A.vx_x, n, thr2, A.part0, red);
-    grid_sync(A.bar);
+    grid_sync(A.bar, p);
     // vx_x[density < thr2] = fill (deposit.py:232) and the sum of vx_x for
     // its mean, in one pass over the reduction's element assignment
     double fill;
@@ -437,15 +449,17 @@ df_stage(DfArgs A) {
             A.part1[vb * 2 + 1] = 0.0;
         }
     }
-    grid_sync(A.bar);
+    grid_sync(A.bar, p);
     if (blockIdx.x == 0) {
         double s, c;
         reduce_combine<2>(A.part1, tile, s, c);
         if (threadIdx.x == 0) {
             sc[4] = s / (double)n;
-            if (*(volatile unsigned int *)&A.bar->err != 0u) {
+            const bool failed = *(volatile unsigned int *)&A.bar->err != 0u;
+            if (failed) {
                 for (int k = 0; k < 7; ++k) sc[k] = __longlong_as_double(0x7ff8000000000000ll);
             }
+            sc[7] = failed ? 1.0 : 0.0;
         }
     }
 }
@@ -497,6 +511,10 @@ extern "C" int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, doub
     DFCSR_CHECK_ARG(p->sg_coeff && p->sg_lo && p->sg_hi && p->gx && p->gz && p->dxg && p->dzg,
                     "dfcsr_df_finalize: null parameter array");
     DFCSR_CHECK_ARG(nz <= 16384, "dfcsr_df_finalize: at most 16384 z bins (got %d)", nz);
+    DFCSR_CHECK_ARG(p->barrier_extra == 0 || p->barrier_extra == 1,
+                    "dfcsr_df_finalize: barrier_extra must be 0 or 1 (got %d)", p->barrier_extra);
+    DFCSR_CHECK_ARG(p->barrier_spins <= kBarSpins,
+                    "dfcsr_df_finalize: barrier_spins must be at most %u (got %u)", kBarSpins, p->barrier_spins);
     const size_t need = dfcsr_df_workspace_bytes(nx, nz);
     if (!workspace || workspace_bytes < need) {
         set_error("dfcsr_df_finalize: workspace too small (%zu < %zu)", workspace_bytes, need);
@@ -517,10 +535,18 @@ extern "C" int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, doub
     A.bar = c.take<GridBar>(1);
 
     const int smem = (int)df_smem_bytes(p->window, nz);
-    static int smem_set = 48 * 1024;
-    if (smem > smem_set) {
-        DFCSR_CUDA_TRY(cudaFuncSetAttribute(df_stage, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        smem_set = smem;
+    {
+        // the dynamic shared-memory limit is a per-device function attribute
+        static std::mutex mu;
+        static int smem_set[64];
+        int dev = 0;
+        DFCSR_CUDA_TRY(cudaGetDevice(&dev));
+        DFCSR_CHECK_ARG(dev >= 0 && dev < 64, "dfcsr_df_finalize: device ordinal %d out of range", dev);
+        std::lock_guard<std::mutex> g(mu);
+        if (smem > 48 * 1024 && smem > smem_set[dev]) {
+            DFCSR_CUDA_TRY(cudaFuncSetAttribute(df_stage, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            smem_set[dev] = smem;
+        }
     }
     // every CTA must be resident at once: a cooperative launch no larger than
     // the occupancy allows

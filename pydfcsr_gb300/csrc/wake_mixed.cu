@@ -31,6 +31,8 @@
 //  * band kernel (FP64, optional): s' columns with |s' - s| < near_band are
 //    skipped by the integral kernel and evaluated with the FP64 integrand.
 //  * finalize kernel: adds the regions in the reference's order and scales.
+#include <mutex>
+
 #include "dw.cuh"
 #include "wake_common.cuh"
 
@@ -1077,17 +1079,42 @@ static size_t mixed_carve(Carver &c, const MixedLayout &L, unsigned long long **
     return c.used;
 }
 
-static int integral_blocks(size_t smem) {
-    static size_t cached_smem = 0;
-    static int cached = 0;
-    if (cached && cached_smem == smem) return cached;
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mixed_integral, MX_THREADS, smem) !=
-            cudaSuccess || per_sm < 1)
-        per_sm = 1;
-    cached = per_sm * num_sms();
-    cached_smem = smem;
-    return cached;
+// Launch set-up of the integral kernel, per device (the shared-memory
+// attribute is a per-device setting, the occupancy depends on the device):
+// one entry per device ordinal, filled on the device's first call.
+struct IntegralDevState {
+    bool attr;
+    size_t smem;
+    int blocks;
+};
+constexpr int kMaxDevices = 64;
+static std::mutex g_integral_mu;
+static IntegralDevState g_integral_dev[kMaxDevices];
+
+static int integral_setup(size_t smem, int *blocks) {
+    int dev = 0;
+    DFCSR_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("dfcsr_wake_mixed: device ordinal %d out of range", dev);
+        return DFCSR_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> g(g_integral_mu);
+    IntegralDevState &d = g_integral_dev[dev];
+    if (!d.attr) {
+        DFCSR_CUDA_TRY(cudaFuncSetAttribute(mixed_integral, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)integral_smem_bytes(MX_MAX_ROWS)));
+        d.attr = true;
+    }
+    if (d.blocks == 0 || d.smem != smem) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mixed_integral, MX_THREADS, smem) !=
+                cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        d.blocks = per_sm * num_sms();
+        d.smem = smem;
+    }
+    *blocks = d.blocks;
+    return DFCSR_OK;
 }
 
 }  // namespace dfcsr
@@ -1133,15 +1160,13 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
         return DFCSR_OOM;
     }
     cudaStream_t st = as_stream(stream);
-    static bool attr_set = false;
-    if (!attr_set) {
-        DFCSR_CUDA_TRY(cudaFuncSetAttribute(mixed_integral, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)integral_smem_bytes(MX_MAX_ROWS)));
-        attr_set = true;
-    }
     const int max_rows = 2 * xbins_max;
     const size_t smem = integral_smem_bytes(max_rows);
-    const int blocks_max = integral_blocks(smem);
+    int blocks_max = 0;
+    {
+        const int rc = integral_setup(smem, &blocks_max);
+        if (rc != DFCSR_OK) return rc;
+    }
     int64_t setup_first = 0, setup_count = 0;
     for (int64_t first = 0; first < n; first += L.batch) {
         const int64_t count = (n - first < L.batch) ? n - first : L.batch;

@@ -185,6 +185,16 @@ class PendingDeposit:
         self.moments, self.fields, self.event = moments, fields, event
 
 
+def raise_if_df_failed(flags):
+    """Raise DfcsrTimeout if any DF finalisation status word in ``flags``
+    (host values of scalars[7]) is set."""
+    bad = int(np.count_nonzero(np.asarray(flags) != 0.0))
+    if bad:
+        raise _lib.DfcsrTimeout(3, "dfcsr_df_finalize",
+                                f"a grid-barrier wait gave up in {bad} DF finalisation(s); "
+                                "their fields are invalid")
+
+
 class _DFEntry:
     """One logged DF: grids (numpy linspaces and their (start, stop, n)),
     the five fields on the device, the finalisation scalars, t and sigmas."""
@@ -239,6 +249,15 @@ class DF_tracker:
         self._cur = None
         self.stats = None
         self.reinterpolated = False
+        # finalisation scalars not yet checked for a barrier timeout:
+        # [(scalars, event after the finalisation)]
+        self._unchecked = []
+        # (extension) test hooks of the DF stage's bounded grid-barrier waits:
+        # polls before a wait gives up (0: the library's default, about a
+        # second) and 1 to expect an arrival that never comes, so that the
+        # waits run out and the timeout path is exercised
+        self.barrier_spins = 0
+        self.barrier_extra = 0
 
     def configure_params(self, xbins=100, zbins=100, xlim=5, zlim=5, filter_order=0,
                          filter_window=0, velocity_threhold=5, upper_limit=None):
@@ -346,12 +365,38 @@ class DF_tracker:
         (P.sg_coeff, P.sg_lo, P.sg_hi, P.gx, P.gz, P.dxg, P.dzg) = [base + 8 * int(o) for o in offs[:7]]
         P.gx_uniform, P.gz_uniform = int(gxu), int(gzu)
         P.gx_dx, P.gz_dx = gxdx, gzdx
+        P.barrier_spins, P.barrier_extra = int(self.barrier_spins), int(self.barrier_extra)
         need = _lib.query("dfcsr_df_workspace_bytes", xb, zb)
         buf = ws.get("df", need)
         _lib.call("dfcsr_df_finalize", ctypes.byref(P), ptr(fields[0]), ptr(fields[3]),
                   ptr(fields[1]), ptr(fields[2]), ptr(fields[4]), ptr(sc), ptr(buf), buf.numel(),
                   stream_handle(stream))
         self._blob = blob   # keep the constants alive until the stream consumes them
+        ev = torch.cuda.Event()
+        ev.record(stream if stream is not None else torch.cuda.current_stream())
+        self._unchecked.append((sc, ev))
+        if len(self._unchecked) > 256:   # a caller that never checks: bound the list
+            self.check_status()
+
+    def take_unchecked(self):
+        """(extension) The finalisation scalars not yet checked, as
+        [(scalars, event)], handed over to the caller (who checks their
+        status word, scalars[7], once the events have passed)."""
+        out, self._unchecked = self._unchecked, []
+        return out
+
+    def check_status(self):
+        """(extension) Raise :class:`DfcsrTimeout` if a DF finalisation since
+        the last check reported that one of its grid-barrier waits gave up
+        (status word scalars[7] = 1: that step's fields are invalid).  Waits
+        for those finalisations."""
+        pend = self.take_unchecked()
+        if not pend:
+            return
+        for _, ev in pend:
+            ev.synchronize()
+        flags = torch.stack([sc[7] for sc, _ in pend]).cpu().numpy()
+        raise_if_df_failed(flags)
 
     # compatibility views of the current DF (host copies)
     def _field(self, name):

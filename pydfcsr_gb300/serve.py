@@ -234,6 +234,13 @@ class _Live:
             self.done_event = torch.cuda.Event()
             self.done_event.record(self.stream)
 
+    def check(self):
+        """Raise DfcsrTimeout if a DF finalisation of this request reported
+        a grid-barrier wait that gave up (waits for this request's DF work)."""
+        import torch
+        with torch.cuda.stream(self.stream):
+            self.csr.DF_tracker.check_status()
+
     def wants_wake(self):
         return self.k >= 2        # the interpolant needs two history slices
 
@@ -400,8 +407,9 @@ class WakeServer:
     def _clock(self):
         return time.perf_counter() - self.t0
 
-    def _wake_tick(self, reqs):
-        """One batched wake launch for every request in `reqs`."""
+    def _wake_tick(self, reqs, errs):
+        """One batched wake launch for every request in `reqs`; a request
+        whose DF step failed gets no result and fails alone."""
         from .CSR import wake_job
         if not reqs:
             return
@@ -424,6 +432,12 @@ class WakeServer:
         for lv in reqs:
             shape = (lv.csr.CSR_params.xbins, lv.csr.CSR_params.zbins)
             m = shape[0] * shape[1]
+            try:
+                lv.check()              # a failed DF step: this request's points are invalid
+            except errs as e:
+                self._fail(lv.spec, e, lv)
+                off += m
+                continue
             lv.results.append((lv.k, dE[off:off + m].reshape(shape), xk[off:off + m].reshape(shape)))
             lv.points += m
             off += m
@@ -472,11 +486,13 @@ class WakeServer:
             lives = self._each(lives, "advance_finish", errs)
             tick = [lv for lv in lives if lv.wants_wake()]
             try:
-                self._wake_tick(tick)
+                self._wake_tick(tick, errs)
             except errs as e:                   # the shared launch: all its requests
                 for lv in tick:
-                    self._fail(lv.spec, e, lv)
-                lives = [lv for lv in lives if not lv.failed]
+                    if not lv.failed:
+                        self._fail(lv.spec, e, lv)
+            lives = [lv for lv in lives if not lv.failed]
+            lives = self._each(lives, "check", errs)   # the DF steps of requests without a wake
             self.ticks += 1
             for lv in lives:
                 if lv.last_step():

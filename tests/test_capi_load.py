@@ -61,6 +61,22 @@ def test_status_names_and_sizes():
     assert lib.dfcsr_wake_workspace_bytes(100, 100, 4096) > 0
 
 
+def test_noalloc_limits_fit_its_array():
+    """The no-alloc deposit's stated maximum (2^20 particles, 256 x 256 grid)
+    needs no more scratch than its fixed array holds; grids whose key count
+    overflows int are refused, not wrapped."""
+    lib = _lib.load()
+    assert 0 < lib.dfcsr_deposit_workspace_bytes(1 << 20, 256, 256) <= \
+        lib.dfcsr_deposit_noalloc_max_bytes()
+    assert lib.dfcsr_deposit_workspace_bytes(1000, 2 ** 31 - 1, 4) == 0
+    with pytest.raises(_lib.DfcsrBadArgument, match="no-alloc maximum"):
+        _lib.call("dfcsr_deposit_cic2d_noalloc", None, None, None, None, 10, 2 ** 31 - 1, 0.0,
+                  1.0, 4, 0.0, 1.0, None, None, None)
+    with pytest.raises(_lib.DfcsrBadArgument, match="too large"):
+        _lib.call("dfcsr_deposit_cic2d", None, None, None, None, 10, 2 ** 31 - 1, 0.0, 1.0, 4,
+                  0.0, 1.0, ctypes.c_void_p(16), None, None, 0, None)
+
+
 def test_bad_arguments_fail_without_gpu():
     """Argument checks run before any device work, so they are testable here."""
     with pytest.raises(_lib.DfcsrBadArgument):

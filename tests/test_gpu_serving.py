@@ -133,3 +133,39 @@ def test_kernel_error_fails_one_request_only(monkeypatch):
         for (k, dE1, xk1), (_, dE2, xk2) in zip(got, want):
             assert np.array_equal(dE1, dE2) and np.array_equal(xk1, xk2), (sp.id, k)
 
+
+
+def test_df_barrier_timeout_fails_one_request_only(monkeypatch):
+    """A DF finalisation whose grid-barrier waits run out (one request's
+    step 3 expects an arrival that never comes, with a short spin limit):
+    the device reports it in the stage's status word, that request fails
+    with a timeout and gets no result for the step, and the other requests'
+    results are bitwise those of a run without it."""
+    from pydfcsr_gb300.serve import WakeServer, _Live
+    specs = _stream()[:3]
+    bad = specs[1].id
+    real = _Live.advance_finish
+
+    def advance_finish(self):
+        if self.spec.id == bad and self.k == 3:
+            tr = self.csr.DF_tracker
+            tr.barrier_spins, tr.barrier_extra = 1 << 14, 1
+        return real(self)
+
+    monkeypatch.setattr(_Live, "advance_finish", advance_finish)
+    srv = WakeServer(specs, max_active=3, chunk=256)
+    summ = srv.run()
+    monkeypatch.undo()
+    assert summ["failed"] == 1 and summ["refused"] == 0
+    assert "TIMEOUT" in srv.failed()[bad]
+    assert srv.sched.admission.used == 0 and srv.sched.admission.active == 0
+    assert [k for k, _, _ in srv.result(bad)] == [2]
+    ref = WakeServer([sp for sp in specs if sp.id != bad], max_active=3, chunk=256)
+    ref.run()
+    for sp in specs:
+        if sp.id == bad:
+            continue
+        got, want = srv.result(sp.id), ref.result(sp.id)
+        assert [k for k, _, _ in got] == [k for k, _, _ in want] == [2, 3, 4]
+        for (k, dE1, xk1), (_, dE2, xk2) in zip(got, want):
+            assert np.array_equal(dE1, dE2) and np.array_equal(xk1, xk2), (sp.id, k)

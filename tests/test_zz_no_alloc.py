@@ -48,8 +48,11 @@ def _maxrel(a, b):
 
 @cuda
 def test_noalloc_matches_workspace_entry_two_calls():
-    # first call: large case; second call: fewer particles on a different grid
-    for n, nb1, nb2, seed in ((1_000_000, 256, 256, 1), (70_000, 40, 200, 2)):
+    # the stated maximum (2^20 particles on a 256 x 256 grid) fits the array
+    lib = _lib.load()
+    assert lib.dfcsr_deposit_workspace_bytes(1 << 20, 256, 256) <= lib.dfcsr_deposit_noalloc_max_bytes()
+    # first call: the maximum; second call: fewer particles on a different grid
+    for n, nb1, nb2, seed in ((1 << 20, 256, 256, 1), (70_000, 40, 200, 2)):
         x, z, w, g = _case(n, nb1, nb2, seed)
         a0, a1 = _noalloc(x, z, None, w, *g)
         b0, b1 = deposit_cic(x, z, None, w, *g)
