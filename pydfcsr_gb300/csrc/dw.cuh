@@ -94,6 +94,46 @@ __device__ __forceinline__ dw dw_sqrt(dw x) {
     return fast_two_sum(s, __fdiv_rn(r, __fmul_rn(2.f, s)));
 }
 
+// x + y when only the absolute error matters, or when x and y have the same
+// sign (Dekker's add: one TwoSum on the high parts, the low parts added in
+// FP32): |error| <= about 2^-47 * (|x| + |y|), i.e. it may lose relative
+// accuracy under cancellation but never absolute accuracy.
+__device__ __forceinline__ dw dw_add_abs(dw x, dw y) {
+    const dw s = two_sum(x.hi, y.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+
+__device__ __forceinline__ dw dw_sub_abs(dw x, dw y) { return dw_add_abs(x, dw_neg(y)); }
+
+// quotient of double-words: the FP32 quotient corrected by one step on the
+// double-word remainder x - q y.
+__device__ __forceinline__ dw dw_div(dw x, dw y) {
+    const float q = __fdiv_rn(x.hi, y.hi);
+    const dw p = dw_mul_f(y, q);
+    const dw r = dw_sub(x, p);
+    return fast_two_sum(q, __fdiv_rn(r.hi, y.hi));
+}
+
+// Square root and reciprocal square root of a positive double-word x from
+// one hardware reciprocal square root y ~ 1/sqrt(x.hi) (a few ulp): the root
+// is s + (x - s^2) y / 2 with s = x.hi y (one Newton step on the exact
+// double-word residual, ~2^-46 relative); *inv_root gets y (FP32 accuracy).
+__device__ __forceinline__ dw dw_sqrt_rsq(dw x, float *inv_root) {
+    const float y = rsqrtf(x.hi);
+    const float s = __fmul_rn(x.hi, y);
+    const dw p = two_prod(s, s);
+    const float res = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, p.hi), p.lo), x.lo);
+    *inv_root = y;
+    return fast_two_sum(s, __fmul_rn(__fmul_rn(0.5f, res), y));
+}
+
+// reciprocal of a positive double-word x given y ~ 1/x.hi (a few ulp): one
+// Newton step y + y (1 - x y), the residual 1 - x y formed with FMAs.
+__device__ __forceinline__ dw dw_recip_from(dw x, float y) {
+    const float e = __fsub_rn(__fmaf_rn(-x.hi, y, 1.f), __fmul_rn(x.lo, y));
+    return fast_two_sum(y, __fmul_rn(y, e));
+}
+
 // floor of the double-word value as a double-word integer (hi + lo is the
 // exact value; floor(hi) can be off by one when hi is an integer and lo < 0,
 // or when hi is so large that lo carries the fraction)

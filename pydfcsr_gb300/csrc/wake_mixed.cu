@@ -46,18 +46,23 @@ constexpr int GEO_THREADS = 128;
 constexpr int SETUP_THREADS = 64;
 constexpr int GEO_MAXB = 6;
 
-// Column record: 28 words (7 float4; stride 112 B keeps 8-lane phases of
-// 16-byte shared loads conflict free).  Row record: 8 words (2 float4).
-constexpr int CW = 28;
+// Column record: 36 words (9 float4; a stride of 144 B keeps 8-lane phases
+// of 16-byte shared loads conflict free).  Row record: 8 words (2 float4).
+constexpr int CW = 36;
 constexpr int RW = 8;
-// column record words (float4 groups):
-//  0: t cell (int), z cell (int), t offset, z offset
-//  1: |R0|, R0.n', |n'|^2 - 1, curvature at s'
-//  2: v.tau' (a), v.n' (b), tau'.n' (e), |n'|^2 (g)
-//  3: |tau'|^2 (h), K0x = b - a e, K1x - 1 = a g - 1 + b e, K2x = b g
-//  4: K0z = a (1 - h), K1z = a e + b h, K2z = b e, Q0 = R0.(n - n')
-//  5: Q1 = n'.(n - n'), q2 = n.tau', M0 = Q0 - q2 |R0|, trapz weight in s'
-// row record words: x0 (int), x weight, u = x' - x'_ref, x' | trapz weight in x', x1 - x0 (int)
+// column record words (float4 groups); "dw" = double-word (hi, lo):
+//  0: t cell (int), z cell (int), t offset (dw)        history coordinates at x'_ref
+//  1: z offset (dw), r0 = |R0| (dw)                    R0 = r(s) + x n(s) - r(s') - x'_ref n(s')
+//  2: u* = R0.n' / g (dw), rmin^2 = (R0 x n')^2 / g (dw)   foot of the perpendicular from
+//     the observer to the line x' -> r(s') + x' n(s'): |r - r'|^2 = rmin^2 + g (u - u*)^2
+//  3: g - 1, K0x = b - a e (dw), curvature at s'       g = |n'|^2
+//  4: a = v.tau', b = v.n', e = tau'.n', h = |tau'|^2
+//  5: K1x - 1 = a g - 1 + b e, K2x = b g, K0z = a (1 - h), K1z = a e + b h
+//  6: K2z = b e, Q0 = R0.(n - n'), Q1 = n'.(n - n'), q2 = n.tau'
+//  7: M0 = Q0 - q2 r0, trapz weight in s', 0, 0
+//  8: 0, 0, 0, 0
+// row record words: x0 (int), x weight, u = x' - x'_ref (dw) | trapz weight in x',
+// x1 - x0 (int), x', 0
 
 struct RegionMeta {
     int nxp, nsp, col_off, row_off;   // offsets in words within the point record
@@ -65,7 +70,7 @@ struct RegionMeta {
 
 struct PointMeta {
     int nreg, valid;
-    float inv_dt, inv_dz;   // FP32 reciprocals of the history t and z steps
+    float inv_dt_hi, inv_dt_lo, inv_dz_hi, inv_dz_lo;   // reciprocals of the history t and z steps (dw)
     RegionMeta reg[WAKE_MAX_REGIONS];
 };
 
@@ -153,7 +158,6 @@ struct alignas(16) GeoShared {
     float wsf[WAKE_MAX_REGIONS][2], wxf[WAKE_MAX_REGIONS][2];
     float rhof[WAKE_MAX_REGIONS][GEO_MAXB + 1];
     float band_f;
-    float inv_dt_f, inv_dz_f;   // FP32 reciprocals of the history t and z steps
     double inv_s, inv_x;        // reciprocals of the orbit-table and history x steps
 };
 
@@ -221,20 +225,25 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
     }
     const bool near = gs.band_f > 0.f && fabsf(dw_float(dw_sub(spj, gs.Sw))) < gs.band_f;
     const float ws = (j == 0 || j == gs.ax_s[r].n - 1) ? gs.wsf[r][0] : gs.wsf[r][1];
+    const dw R0n = dw_add(dw_mul(rx0, npx), dw_mul(ry0, npy));
+    const dw cr = dw_sub(dw_mul(rx0, npy), dw_mul(ry0, npx));
+    const dw us = dw_div(R0n, g);
+    const dw rmin2 = dw_div(dw_mul(cr, cr), g);
+    const dw toff = dw_add_f(ut0, -tfl), zoff = dw_add_f(uz0, -zfl);
+    const dw K0x = dw_sub(bb, ae);
     o[0] = make_float4(__int_as_float(cell_of(tfl, dw_isnan(ut0))),
-                       __int_as_float(cell_of(zfl, dw_isnan(uz0))),
-                       dw_float(dw_add_f(ut0, -tfl)), dw_float(dw_add_f(uz0, -zfl)));
-    o[1] = make_float4(dw_float(r0), dw_float(dw_add(dw_mul(rx0, npx), dw_mul(ry0, npy))),
-                       dw_float(dw_add_f(g, -1.f)), rho_f);
-    o[2] = make_float4(dw_float(a), dw_float(bb), dw_float(e), dw_float(g));
-    o[3] = make_float4(dw_float(h), dw_float(dw_sub(bb, ae)),
-                       dw_float(dw_add(dw_add_f(dw_mul(a, g), -1.f), dw_mul(bb, e))),
-                       dw_float(dw_mul(bb, g)));
-    o[4] = make_float4(dw_float(dw_mul(a, dw_add_f(dw_neg(h), 1.f))), dw_float(dw_add(ae, dw_mul(bb, h))),
-                       dw_float(dw_mul(bb, e)), dw_float(Q0));
-    o[5] = make_float4(dw_float(dw_add(dw_mul(npx, nmx), dw_mul(npy, nmy))), dw_float(q2),
-                       dw_float(dw_sub(Q0, dw_mul(q2, r0))),
-                       near ? 0.f : ws);   // band columns: FP64 kernel
+                       __int_as_float(cell_of(zfl, dw_isnan(uz0))), toff.hi, toff.lo);
+    o[1] = make_float4(zoff.hi, zoff.lo, r0.hi, r0.lo);
+    o[2] = make_float4(us.hi, us.lo, rmin2.hi, rmin2.lo);
+    o[3] = make_float4(dw_float(dw_add_f(g, -1.f)), K0x.hi, K0x.lo, rho_f);
+    o[4] = make_float4(dw_float(a), dw_float(bb), dw_float(e), dw_float(h));
+    o[5] = make_float4(dw_float(dw_add(dw_add_f(dw_mul(a, g), -1.f), dw_mul(bb, e))),
+                       dw_float(dw_mul(bb, g)), dw_float(dw_mul(a, dw_add_f(dw_neg(h), 1.f))),
+                       dw_float(dw_add(ae, dw_mul(bb, h))));
+    o[6] = make_float4(dw_float(dw_mul(bb, e)), dw_float(Q0),
+                       dw_float(dw_add(dw_mul(npx, nmx), dw_mul(npy, nmy))), dw_float(q2));
+    o[7] = make_float4(dw_float(dw_sub(Q0, dw_mul(q2, r0))), near ? 0.f : ws, 0.f, 0.f);   // band columns: FP64 kernel
+    o[8] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // One x' row record in double-word FP32: history x cell with the reference's
@@ -256,9 +265,10 @@ __device__ __forceinline__ void row_dw(const dfcsr_wake_job &J, GeoShared &gs, i
         xw = dw_float(dw_add_f(ux, -(float)x0));
     }
     const int n = gs.ax_x[r].n;
-    rb[2 * i] = make_float4(__int_as_float(x0), xw, dw_float(dw_sub(xpi, gs.xrefw[r])), dw_float(xpi));
+    const dw u = dw_sub(xpi, gs.xrefw[r]);
+    rb[2 * i] = make_float4(__int_as_float(x0), xw, u.hi, u.lo);
     rb[2 * i + 1] = make_float4((i == 0 || i == n - 1) ? gs.wxf[r][0] : gs.wxf[r][1],
-                                __int_as_float(x1 - x0), 0.f, 0.f);
+                                __int_as_float(x1 - x0), dw_float(xpi), 0.f);
     if (in) {
         atomicMin(&gs.lo[r], i);   // integer min / max: order independent
         atomicMax(&gs.hi[r], i);
@@ -332,16 +342,20 @@ __device__ __noinline__ void geometry_fp64(const dfcsr_wake_job &J, GeoShared &g
         const double q2 = nsx * tpx + nsy * tpy;
         const bool near = J.near_band > 0.0 && fabs(spj - s) < J.near_band;
         float4 *o = reinterpret_cast<float4 *>(prec + gs.rm[r].col_off) + (size_t)j * (CW / 4);
+        const double R0n = rx0 * npx + ry0 * npy, cr = rx0 * npy - ry0 * npx;
+        const dw toff = dw_from(ut0 - tfl), zoff = dw_from(uz0 - zfl), r0w = dw_from(r0);
+        const dw us = dw_from(R0n / g), rmin2 = dw_from(cr * cr / g), K0x = dw_from(bb - a * e);
         o[0] = make_float4(__int_as_float(cell_index(ut0, tfl)), __int_as_float(cell_index(uz0, zfl)),
-                           (float)(ut0 - tfl), (float)(uz0 - zfl));
-        o[1] = make_float4((float)r0, (float)(rx0 * npx + ry0 * npy), (float)(g - 1.0), rho_f);
-        o[2] = make_float4((float)a, (float)bb, (float)e, (float)g);
-        o[3] = make_float4((float)h, (float)(bb - a * e), (float)((a * g - 1.0) + bb * e),
-                           (float)(bb * g));
-        o[4] = make_float4((float)(a * (1.0 - h)), (float)(a * e + bb * h), (float)(bb * e),
-                           (float)Q0);
-        o[5] = make_float4((float)(npx * nmx + npy * nmy), (float)q2, (float)(Q0 - q2 * r0),
-                           near ? 0.f : (float)ax_s.weight(j));   // band columns: FP64 kernel
+                           toff.hi, toff.lo);
+        o[1] = make_float4(zoff.hi, zoff.lo, r0w.hi, r0w.lo);
+        o[2] = make_float4(us.hi, us.lo, rmin2.hi, rmin2.lo);
+        o[3] = make_float4((float)(g - 1.0), K0x.hi, K0x.lo, rho_f);
+        o[4] = make_float4((float)a, (float)bb, (float)e, (float)h);
+        o[5] = make_float4((float)((a * g - 1.0) + bb * e), (float)(bb * g), (float)(a * (1.0 - h)),
+                           (float)(a * e + bb * h));
+        o[6] = make_float4((float)(bb * e), (float)Q0, (float)(npx * nmx + npy * nmy), (float)q2);
+        o[7] = make_float4((float)(Q0 - q2 * r0), near ? 0.f : (float)ax_s.weight(j), 0.f, 0.f);   // band columns: FP64 kernel
+        o[8] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     // rows: x cell, offset, u = x' - x'_ref, x', trapz weight; valid row range
     for (int c = threadIdx.x; c < nrows; c += blockDim.x) {
@@ -358,8 +372,9 @@ __device__ __noinline__ void geometry_fp64(const dfcsr_wake_job &J, GeoShared &g
         double xw = 0.0;
         const bool in = axis_index(ux, J.nx, x0, x1, xw);
         float4 *rb = reinterpret_cast<float4 *>(prec + gs.rm[r].row_off);
-        rb[2 * i] = make_float4(__int_as_float(x0), (float)xw, (float)(xpi - gs.xref[r]), (float)xpi);
-        rb[2 * i + 1] = make_float4((float)ax_x.weight(i), __int_as_float(x1 - x0), 0.f, 0.f);
+        const dw u = dw_from(xpi - gs.xref[r]);
+        rb[2 * i] = make_float4(__int_as_float(x0), (float)xw, u.hi, u.lo);
+        rb[2 * i + 1] = make_float4((float)ax_x.weight(i), __int_as_float(x1 - x0), (float)xpi, 0.f);
         if (in) {
             atomicMin(&gs.lo[r], i);   // integer min / max: order independent
             atomicMax(&gs.hi[r], i);
@@ -471,6 +486,8 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
         }
         const dw dd = dw_from(dv);
         if (l == 11) gs.vxw = dd;
+        if (l == 8) gs.inv_t = dd;   // the integral needs these for every job
+        if (l == 9) gs.inv_z = dd;
         if (use_dw) {
             switch (l) {
                 case 0: gs.Px = dd; break;
@@ -481,15 +498,11 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
                 case 5: gs.tsy = dd; break;
                 case 6: gs.T0 = dd; break;
                 case 7: gs.Tz = dd; break;
-                case 8: gs.inv_t = dd; break;
-                case 9: gs.inv_z = dd; break;
                 case 10: gs.Sw = dd; break;
                 default: break;
             }
         }
         if (l == 12) {
-            gs.inv_dt_f = (float)qv[4];
-            gs.inv_dz_f = (float)qv[5];
             gs.inv_s = qv[6];
             gs.inv_x = qv[7];
             gs.band_f = (use_dw && J.near_band > 0.0) ? (float)J.near_band : 0.f;
@@ -638,8 +651,10 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         PointMeta m;
         m.nreg = gs.nreg;
         m.valid = gs.ok;
-        m.inv_dt = gs.inv_dt_f;
-        m.inv_dz = gs.inv_dz_f;
+        m.inv_dt_hi = gs.inv_t.hi;
+        m.inv_dt_lo = gs.inv_t.lo;
+        m.inv_dz_hi = gs.inv_z.hi;
+        m.inv_dz_lo = gs.inv_z.lo;
         for (int k = 0; k < WAKE_MAX_REGIONS; ++k)
             m.reg[k] = (k < gs.nreg) ? gs.rm[k] : RegionMeta{0, 0, 0, 0};
         meta[b] = m;
@@ -675,21 +690,28 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         rows_valid[b * WAKE_MAX_REGIONS + threadIdx.x] = make_int2(gs.lo[threadIdx.x], gs.hi[threadIdx.x] + 1);
 }
 
-// Resolve one axis from an integer base and an FP32 offset with the
-// reference's int() truncation rule (in range iff -1 < u < n).
-__device__ __forceinline__ bool axis_split(int base, float off, int n, int &i0, int &i1, float &w) {
-    const float k = floorf(off);
+// Resolve one axis from an integer base and a double-word offset with the
+// reference's int() truncation rule (in range iff -1 < u < n, u = base +
+// off): the lower index and the FP32 weight.  The range decision uses the
+// double-word value, so it agrees with the FP64 decision except within
+// ~1e-12 cells of a boundary (at u = -1 the reference's interpolant jumps
+// from an extrapolated value to zero).
+__device__ __forceinline__ bool axis_split_dw(int base, dw off, int n, int &i0, int &i1, float &w) {
+    float k = floorf(off.hi);
+    float fr = __fadd_rn(__fsub_rn(off.hi, k), off.lo);   // off.hi - k is exact
+    if (fr < 0.f) { k = __fsub_rn(k, 1.f); fr = __fadd_rn(fr, 1.f); }
+    else if (fr >= 1.f) { k = __fadd_rn(k, 1.f); fr = __fsub_rn(fr, 1.f); }
     const int ui = base + (int)k;
-    const float fr = off - k;
     if (!(ui > -1 || (ui == -1 && fr > 0.f)) || ui >= n) return false;
-    if (ui == -1) { i0 = 0; w = fr - 1.f; }
+    if (ui == -1) { i0 = 0; w = __fsub_rn(fr, 1.f); }
     else { i0 = ui; w = fr; }
     i1 = (i0 == n - 1) ? i0 : i0 + 1;
     return true;
 }
 
 struct Fields5 {
-    float den, dx, dz, vx, vxx;
+    float den, dz, vx, vxx;
+    float dx_h, dx_d;   // density_x = dx_h + dx_d (offset form)
 };
 
 // A 32-byte history cell (den, dx_hi, dz, vx | vxx, dx_lo, pad, pad) in one
@@ -707,9 +729,14 @@ __device__ __forceinline__ float lerp1(float a, float b, float w) { return fmaf(
 
 // Trilinear FP32 gather of the five fields from ring32 [slot][nx][nz][8]
 // (cell: den, dx_hi, dz, vx | vxx, dx_lo, 0, 0), interpolating t, then x,
-// then z like the reference; density_x in float-float when FF.
+// then z like the reference.  density_x (stored as hi + lo) comes back in
+// offset form: the corners enter as (hi_c - h) + lo_c with h the high part
+// of the first corner (the subtraction is exact for neighbouring values
+// within a factor 2), the trilinear chain runs on these small offsets and
+// the value is h + D, unrounded - the wake's density_x term is a sum that
+// cancels to ~1/300 of its terms, and this form keeps it to ~1e-9 of the
+// value instead of an FP32 rounding.
 // c<x><t>: float4 index of the z0 cell at x0/x1, t0/t1; dzc: float4 step to z1.
-template <bool FF>
 __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint32_t c00, uint32_t c01,
                                            uint32_t c10, uint32_t c11, uint32_t dzc, float td, float xd,
                                            float zd) {
@@ -739,21 +766,12 @@ __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint
     r.dz = tri(A0.z, B0.z, A1.z, B1.z, C0.z, D0.z, C1.z, D1.z);
     r.vx = tri(A0.w, B0.w, A1.w, B1.w, C0.w, D0.w, C1.w, D1.w);
     r.vxx = tri(a0.x, b0.x, a1.x, b1.x, c0.x, d0.x, c1.x, d1.x);
-    if (FF) {
-        // density_x stored as hi + lo: interpolate the offsets from the high
-        // part of the first corner, (hi_c - h) + lo_c (the subtraction is
-        // exact for neighbouring values within a factor 2), so the lerp
-        // chain rounds only small numbers and the result h + D is rounded
-        // once - a correctly rounded FP32 value of the FP64 interpolant
-        const float h = A0.y;
-        r.dx = __fadd_rn(h, tri(a0.y, __fadd_rn(__fsub_rn(B0.y, h), b0.y),
-                                __fadd_rn(__fsub_rn(A1.y, h), a1.y), __fadd_rn(__fsub_rn(B1.y, h), b1.y),
-                                __fadd_rn(__fsub_rn(C0.y, h), c0.y), __fadd_rn(__fsub_rn(D0.y, h), d0.y),
-                                __fadd_rn(__fsub_rn(C1.y, h), c1.y), __fadd_rn(__fsub_rn(D1.y, h), d1.y)));
-    } else {
-        r.dx = tri(A0.y + a0.y, B0.y + b0.y, A1.y + a1.y, B1.y + b1.y, C0.y + c0.y, D0.y + d0.y,
-                   C1.y + c1.y, D1.y + d1.y);
-    }
+    const float h = A0.y;
+    r.dx_h = h;
+    r.dx_d = tri(a0.y, __fadd_rn(__fsub_rn(B0.y, h), b0.y), __fadd_rn(__fsub_rn(A1.y, h), a1.y),
+                 __fadd_rn(__fsub_rn(B1.y, h), b1.y), __fadd_rn(__fsub_rn(C0.y, h), c0.y),
+                 __fadd_rn(__fsub_rn(D0.y, h), d0.y), __fadd_rn(__fsub_rn(C1.y, h), c1.y),
+                 __fadd_rn(__fsub_rn(D1.y, h), d1.y));
     return r;
 }
 
@@ -808,22 +826,36 @@ __device__ __forceinline__ void block_sum2_dw(dw &z, dw &x, float4 *red) {
 struct RingView {
     const float4 *ring;
     int nt, nx, nz, head, cap;
-    float inv_dt, inv_dz;
+    dw inv_dt, inv_dz;
+};
+
+// Per-thread sums of one chunk: the density_x term of the longitudinal
+// integrand in double-word (it cancels: its terms sum to ~1/300 of their
+// magnitude, so each term must be accurate well beyond FP32), the rest of
+// the longitudinal integrand and the transverse one as Kahan-compensated
+// FP32 sums.
+struct ChunkSums {
+    dw zx;
+    float sz, cz, sx, cx;
 };
 
 // Integrand contribution of rows [i_lo, i_hi) x columns [0, C) of a chunk.
 // Work unit = one s' column x MX_ROWBLK consecutive x' rows: a warp covers
 // consecutive columns of one row block, so its gathers stay close in the
 // history (neighbouring s' -> neighbouring cells) and the row records it
-// reads are the same for all lanes (shared-memory broadcast); each thread
-// keeps its column record in registers for the rows of its unit.
+// reads are the same for all lanes (shared-memory broadcast).
+//
+// Per integrand point, in double-word: the distance from the perpendicular
+// foot, |r - r'|^2 = rmin^2 + g (u - u*)^2 (no cancellation, unlike
+// r0^2 + D near the source), its change from the column's reference row,
+// delta = |r - r'| - r0, and the history coordinates t = t0 - delta / dt,
+// z = z0 + delta / dz (a z shift reaches ~100 cells near the source, so an
+// FP32 product would misplace the gather by ~1e-5 cell); then the density_x
+// product chain w scale brx dx / |r - r'|.  The other terms are FP32.
 constexpr int MX_ROWBLK = 4;
 
-template <bool FF>
 __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float4 *__restrict__ rows,
-                                             const RingView &V, int i_lo,
-                                             int i_hi, int C, float &sz, float &cz, float &sx,
-                                             float &cx) {
+                                             const RingView &V, int i_lo, int i_hi, int C, ChunkSums &acc) {
     const int nblk = (i_hi - i_lo + MX_ROWBLK - 1) / MX_ROWBLK;
     const int units = nblk * C;
     const int tid = threadIdx.x;
@@ -831,16 +863,21 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
     int rb = tid / C, jl = tid - (tid / C) * C;
     const int drb = MX_THREADS / C, dj = MX_THREADS - (MX_THREADS / C) * C;
     const uint32_t nzc = (uint32_t)V.nz * 2u;   // float4 per x row of a slot
-    for (int u = tid; u < units; u += MX_THREADS) {
+    for (int u0 = tid; u0 < units; u0 += MX_THREADS) {
         const float4 *cr = sm.col + jl * (CW / 4);
         const int i0 = i_lo + rb * MX_ROWBLK;
         rb += drb;
         jl += dj;
         if (jl >= C) { jl -= C; rb += 1; }
-        const float4 q0 = cr[0], q5 = cr[5];
-        const float ws = q5.w;
+        const float4 q7 = cr[7];
+        const float ws = q7.y;
         if (ws == 0.f) continue;
-        const float4 g1 = cr[1], q2 = cr[2], q3 = cr[3], q4 = cr[4];
+        const float4 q0 = cr[0], q1 = cr[1], q2 = cr[2], q3 = cr[3];
+        const int tcell = __float_as_int(q0.x), zcell = __float_as_int(q0.y);
+        const dw toff{q0.z, q0.w}, zoff{q1.x, q1.y}, r0{q1.z, q1.w};
+        const dw us{q2.x, q2.y}, rmin2{q2.z, q2.w};
+        const float gm1 = q3.x, rho = q3.w;
+        const dw K0x{q3.y, q3.z};
         const int iend = min(i0 + MX_ROWBLK, i_hi);
         for (int i = i0; i < iend; ++i) {
             const float4 *rr = rows + i * (RW / 4);
@@ -848,15 +885,24 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
             const float4 rw = rr[1];
             const float wx = rw.x;
             if (wx == 0.f) continue;
-            const float u = ra.z;
-            const float r0 = g1.x;
-            const float Dd = u * ((g1.z + 1.f) * u - 2.f * g1.y);
-            const float rad = fmaf(r0, r0, Dd);
-            const float delta = __fdividef(Dd, r0 + rad * rsqrtf(rad));
+            // |r - r'| and delta (double-word)
+            const dw uu{ra.z, ra.w};
+            const dw v = dw_sub_abs(uu, us);
+            dw v2 = two_prod(v.hi, v.hi);
+            v2.lo = __fmaf_rn(2.f * v.hi, v.lo, v2.lo);
+            v2.lo = __fmaf_rn(gm1, v2.hi, v2.lo);            // g v^2, g = 1 + (g - 1)
+            const dw r2 = dw_add_abs(rmin2, v2);             // both non-negative
+            float inv_r;
+            const dw rd = dw_sqrt_rsq(r2, &inv_r);
+            const dw del = dw_sub_abs(rd, r0);
+            // history coordinates: t shifts by ~1e-3 cell at most (FP32 product),
+            // z by up to ~100 cells (double-word product)
+            const float delf = dw_float(del);
+            const dw ot = dw_add_f(toff, -__fmul_rn(delf, V.inv_dt.hi));
+            const dw oz = dw_add_abs(zoff, dw_mul(del, V.inv_dz));
             int t0, t1, z0, z1;
             float td, zd;
-            if (!axis_split(__float_as_int(q0.x), q0.z - delta * V.inv_dt, V.nt, t0, t1, td) ||
-                !axis_split(__float_as_int(q0.y), q0.w + delta * V.inv_dz, V.nz, z0, z1, zd))
+            if (!axis_split_dw(tcell, ot, V.nt, t0, t1, td) || !axis_split_dw(zcell, oz, V.nz, z0, z1, zd))
                 continue;   // every field is zero outside the history grid
             // x: rows outside the history grid are not in [i_lo, i_hi)
             const int x0 = __float_as_int(ra.x);
@@ -867,27 +913,38 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
             const uint32_t c0x0 = ((uint32_t)s0 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
             const uint32_t c1x0 = ((uint32_t)s1 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
             const uint32_t dxc = (uint32_t)__float_as_int(rw.y) * nzc;
-            const Fields5 F = gather5<FF>(V.ring, c0x0, c1x0, c0x0 + dxc, c1x0 + dxc,
-                                          2u * (uint32_t)(z1 - z0), td, xd, zd);
-            const float inv_r = __fdividef(1.f, r0 + delta);
-            const float scale = fmaf(ra.w, g1.w, 1.f);
+            const Fields5 F = gather5(V.ring, c0x0, c1x0, c0x0 + dxc, c1x0 + dxc,
+                                      2u * (uint32_t)(z1 - z0), td, xd, zd);
             const float vr = F.vx;
-            // brx = (K0x - vx') - vx' (K1x - 1 + vx' K2x); brz = K0z - vx' (K1z + vx' K2z)
-            const float brx = (q3.y - vr) - vr * fmaf(vr, q3.w, q3.z);
-            const float brz = q4.x - vr * fmaf(vr, q4.z, q4.y);
-            const float p1 = fmaf(vr, q2.y, q2.x);
-            const float num = scale * F.dx * brx + F.dz * brz - scale * p1 * F.den * F.vxx;
-            const float Iz = num * inv_r;
-            const float Q1 = q5.x;
-            const float q1 = q4.w - u * Q1;
-            const float M = q5.z - u * Q1 - q5.y * delta;
-            const float e = q2.z;
-            const float pd = -(F.dx * fmaf(vr, q2.w, e) + F.dz * __fdividef(fmaf(vr, e, q3.x), scale)) -
+            const float4 q4 = cr[4], q5 = cr[5];
+            // density_x term: w scale brx dx / |r - r'| in double-word, with
+            // brx = K0x - vr (K1x + vr K2x) and scale = 1 + x' rho
+            const float dsc = __fmul_rn(rw.z, rho);
+            const float db = -vr * fmaf(vr, q5.y, q5.x + 1.f);
+            dw A = dw_add_f(K0x, db);
+            A = dw_add_f(A, __fmul_rn(dsc, A.hi));
+            const dw w = two_prod(wx, ws);
+            const dw dxv = two_sum(F.dx_h, F.dx_d);
+            const dw T = dw_mul(dw_mul(dw_mul(A, w), dxv), dw_recip_from(rd, inv_r));
+            acc.zx = dw_add_abs(acc.zx, T);
+            // the rest of the longitudinal integrand (FP32)
+            const float4 q6 = cr[6];
+            const float scale = 1.f + dsc;
+            const float wf = wx * ws;
+            const float brz = q5.z - vr * fmaf(vr, q6.x, q5.w);
+            const float p1 = fmaf(vr, q4.y, q4.x);
+            const float rest = (F.dz * brz - scale * p1 * F.den * F.vxx) * inv_r;
+            kahan(acc.sz, acc.cz, wf * rest);
+            // transverse integrand (FP32)
+            const float uf = uu.hi;
+            const float dxf = dw_float(dxv);
+            const float q1x = q6.y - uf * q6.z;
+            const float M = q7.x - uf * q6.z - q6.w * delf;
+            const float e = q4.z;
+            const float pd = -(dxf * fmaf(vr, 1.f + gm1, e) + F.dz * __fdividef(fmaf(vr, e, q4.w), scale)) -
                              F.den * F.vxx;
-            const float Ix = scale * inv_r * inv_r * (q1 * inv_r * F.den + pd * M);
-            const float w = wx * ws;
-            kahan(sz, cz, w * Iz);
-            kahan(sx, cx, w * Ix);
+            const float Ix = scale * inv_r * inv_r * (q1x * inv_r * F.den + pd * M);
+            kahan(acc.sx, acc.cx, wf * Ix);
         }
     }
 }
@@ -923,8 +980,8 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
             RingView V;
             V.ring = reinterpret_cast<const float4 *>(J.ring32);
             V.nt = J.nt; V.nx = J.nx; V.nz = J.nz; V.head = J.head; V.cap = J.cap;
-            V.inv_dt = m->inv_dt;
-            V.inv_dz = m->inv_dz;
+            V.inv_dt = dw{m->inv_dt_hi, m->inv_dt_lo};
+            V.inv_dz = dw{m->inv_dz_hi, m->inv_dz_lo};
             const RegionMeta R = m->reg[r];
             const int2 rv = rows_valid[b * WAKE_MAX_REGIONS + r];
             dw reg_z{0.f, 0.f}, reg_x{0.f, 0.f};
@@ -936,13 +993,10 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
                     const float4 *cb = reinterpret_cast<const float4 *>(base + R.col_off) + (size_t)j0 * (CW / 4);
                     for (int k = tid; k < C * (CW / 4); k += blockDim.x) sm.col[k] = cb[k];
                     __syncthreads();
-                    float sz = 0.f, cz = 0.f, sx = 0.f, cx = 0.f;
-                    if (r == 0)
-                        chunk_points<true>(sm, rows, V, rv.x, rv.y, C, sz, cz, sx, cx);
-                    else
-                        chunk_points<false>(sm, rows, V, rv.x, rv.y, C, sz, cz, sx, cx);
+                    ChunkSums acc{dw{0.f, 0.f}, 0.f, 0.f, 0.f, 0.f};
+                    chunk_points(sm, rows, V, rv.x, rv.y, C, acc);
                     // Kahan state s - c exactly as a double-word
-                    dw bz = two_sum(sz, -cz), bx = two_sum(sx, -cx);
+                    dw bz = dw_add(acc.zx, two_sum(acc.sz, -acc.cz)), bx = two_sum(acc.sx, -acc.cx);
                     block_sum2_dw(bz, bx, sm.red);
                     if (tid == 0) { reg_z = dw_add(reg_z, bz); reg_x = dw_add(reg_x, bx); }
                     __syncthreads();

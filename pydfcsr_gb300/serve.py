@@ -178,17 +178,16 @@ class _Live:
     """Device state of one admitted request: its beam, DF history ring,
     workspace and CUDA stream."""
 
-    def __init__(self, spec, admitted_at, precision="mixed"):
+    def __init__(self, spec, admitted_at, precision="mixed", pool=None):
         import torch
         from .beams import Beam
         from .CSR import CSR2D
-        from .runtime import Workspace
         from .synthetic import StepPlan, dipole_lattice, gaussian_beam_device
 
         self.spec = spec
         self.admitted_at = admitted_at
-        self.stream = torch.cuda.Stream()
-        self.ws = Workspace()
+        self.pool = pool if pool is not None else _ResourcePool()
+        self.stream, self.ws = self.pool.take()
         L = spec.rho * spec.angle
         self.lattice = dipole_lattice(spec.rho, L, L / spec.steps,
                                       tail_drift=max(0.02, 20 * spec.sigma_z))
@@ -210,6 +209,15 @@ class _Live:
         self.finished_at = None
         self.done_event = None
         self.failed = False
+        # latency breakdown (seconds): set-up at admission (beam, first DF
+        # step), per-tick host time of its DF steps, its share of the shared
+        # wake launches (their whole duration), graph captures in those
+        # ticks, ticks taken part in
+        self.setup_s = 0.0
+        self.df_s = 0.0
+        self.wake_s = 0.0
+        self.capture_s = 0.0
+        self.ticks = 0
 
     def advance_launch(self):
         """Transport to the next step and enqueue its beam moments on this
@@ -248,8 +256,34 @@ class _Live:
         return self.k >= self.spec.steps
 
     def release(self):
-        """Drop the device state; results stay."""
-        self.beam = self.csr = self.ws = None
+        """Drop the device state (the stream and workspace go back to the
+        pool once this request's work on the stream is done); results stay."""
+        if self.stream is not None:
+            self.stream.synchronize()
+            self.pool.give(self.stream, self.ws)
+        self.beam = self.csr = self.ws = self.stream = None
+
+
+class _ResourcePool:
+    """CUDA streams and workspaces reused from one request to the next
+    (creating them per request costs host time at every admission).  A
+    workspace keeps the buffers of its largest request: the pool holds at
+    most ``limit`` of them."""
+
+    def __init__(self, limit=64):
+        self.free = []
+        self.limit = int(limit)
+
+    def take(self):
+        import torch
+        from .runtime import Workspace
+        if self.free:
+            return self.free.pop()
+        return torch.cuda.Stream(), Workspace()
+
+    def give(self, stream, ws):
+        if len(self.free) < self.limit:
+            self.free.append((stream, ws))
 
 
 class _BatchedWake:
@@ -293,6 +327,8 @@ class _BatchedWake:
         self.graphs = {}
         self.warm = False
         self.replays = 0
+        self.capture_s = 0.0       # host time of graph captures during the stream
+        self.last_capture_s = 0.0
 
     def _launch(self, n, stream):
         import ctypes
@@ -306,6 +342,25 @@ class _BatchedWake:
         else:
             _lib.call("dfcsr_wake_fp64", ptr(self.jobs), ptr(self.jop), ptr(self.s), ptr(self.x), n,
                       ptr(self.dE), ptr(self.xk), h)
+
+    def _capture(self, k, stream):
+        import torch
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            self._launch(k * self.chunk, stream)
+        self.graphs[k] = g
+        return g
+
+    def precapture(self, stream):
+        """Capture the launch of every chunk count up to the buffers'
+        capacity (after one eager launch: the library's one-time set-up),
+        so that no capture happens while requests wait."""
+        if not self.use_graphs or not self.warm:
+            return 0
+        for k in range(1, self.cap // self.chunk + 1):
+            if k not in self.graphs:
+                self._capture(k, stream)
+        return len(self.graphs)
 
     def run(self, jobs_raw, meshes, stream):
         """One tick: the job structs and job index per point go up from
@@ -348,6 +403,7 @@ class _BatchedWake:
                 self.s[n:padded].copy_(self.s[:1].expand(padded - n))
                 self.x[n:padded].copy_(self.x[:1].expand(padded - n))
             k = padded // self.chunk
+            self.last_capture_s = 0.0
             if not self.use_graphs or not self.warm:
                 # the first call runs eagerly: one-time library set-up happens
                 # outside any capture
@@ -356,10 +412,10 @@ class _BatchedWake:
             else:
                 g = self.graphs.get(k)
                 if g is None:
-                    g = torch.cuda.CUDAGraph()
-                    with torch.cuda.graph(g, stream=stream):
-                        self._launch(padded, stream)
-                    self.graphs[k] = g
+                    t0 = time.perf_counter()
+                    g = self._capture(k, stream)
+                    self.last_capture_s = time.perf_counter() - t0
+                    self.capture_s += self.last_capture_s
                 g.replay()
                 self.replays += 1
             self.out_host[0, :n].copy_(self.dE[:n], non_blocking=True)
@@ -377,7 +433,7 @@ class WakeServer:
     """
 
     def __init__(self, specs, precision="mixed", budget_bytes=None, max_active=32,
-                 use_graphs=True, chunk=2048):
+                 use_graphs=True, chunk=2048, precapture=False):
         import torch
         from . import _lib
         from .runtime import require_cuda
@@ -398,11 +454,36 @@ class WakeServer:
         self.wake = _BatchedWake(max_active * mesh_max * mesh_max, max_active, xb, zb, precision,
                                  chunk, use_graphs)
         self.stream = torch.cuda.Stream()
+        self.pool = _ResourcePool(limit=max_active + 4)
         self.live = {}
         self.ticks = 0
         self.launch_points = []
         self.wake_s = 0.0
+        self.precapture_s = 0.0
         _lib.timing_enable(False)    # no event records inside captured graphs
+        if precapture and use_graphs:
+            self._precapture(specs)
+
+    def _precapture(self, specs):
+        """Warm the batched launch with a small request of the stream's
+        integration bins, run alone before the stream starts, then capture
+        the graphs of all chunk counts."""
+        t0 = time.perf_counter()
+        base = specs[0] if specs else RequestSpec(0, 0.0, 5.0, 0.1, 20_000, 30e-6, 64, 8, 1)
+        warm = RequestSpec(**{**base.__dict__, "id": -1, "arrival_s": 0.0, "n": 20_000,
+                              "grid": 64, "mesh": 8, "steps": 2, "seed": 12345})
+        lv = _Live(warm, 0.0, self.precision, self.pool)
+        lv.advance_launch()
+        lv.advance_finish()
+        lv.advance_launch()
+        lv.advance_finish()
+        self._wake_tick([lv], _request_errors())
+        lv.release()
+        self.wake.precapture(self.stream)
+        self.stream.synchronize()
+        self.wake_s = 0.0
+        self.launch_points = []
+        self.precapture_s = time.perf_counter() - t0
 
     def _clock(self):
         return time.perf_counter() - self.t0
@@ -426,8 +507,12 @@ class WakeServer:
             self.stream.wait_event(lv.done_event)
         t = time.perf_counter()
         dE, xk = self.wake.run(b"".join(bytes(j) for j in jobs), meshes, self.stream)
-        self.wake_s += time.perf_counter() - t
+        dt = time.perf_counter() - t
+        self.wake_s += dt
         self.launch_points.append(dE.size)
+        for lv in reqs:
+            lv.wake_s += dt
+            lv.capture_s += self.wake.last_capture_s
         off = 0
         for lv in reqs:
             shape = (lv.csr.CSR_params.xbins, lv.csr.CSR_params.zbins)
@@ -469,8 +554,10 @@ class WakeServer:
         sched = self.sched
         while not sched.finished():
             for spec in sched.admit():
+                t = time.perf_counter()
                 try:
-                    self.live[spec.id] = _Live(spec, self._clock(), self.precision)
+                    self.live[spec.id] = _Live(spec, self._clock(), self.precision, self.pool)
+                    self.live[spec.id].setup_s = time.perf_counter() - t
                 except errs as e:
                     self._fail(spec, e)
             if not sched.active:
@@ -482,8 +569,13 @@ class WakeServer:
             # every request's transport + moments first, then each request's
             # DF step: the moments of all beams run while the host waits for
             # the first one
+            t = time.perf_counter()
             lives = self._each(lives, "advance_launch", errs)
             lives = self._each(lives, "advance_finish", errs)
+            dt = time.perf_counter() - t
+            for lv in lives:
+                lv.df_s += dt
+                lv.ticks += 1
             tick = [lv for lv in lives if lv.wants_wake()]
             try:
                 self._wake_tick(tick, errs)
@@ -502,20 +594,54 @@ class WakeServer:
         torch.cuda.synchronize()
         return self.summary(self._clock())
 
+    def latency_breakdown(self):
+        """Per finished request: latency (arrival to last result) and its
+        parts - queue (arrival to admission), set-up (beam and first DF step
+        at admission), DF steps (host time of the ticks it took part in),
+        wake (duration of the shared launches it took part in), graph
+        captures within those, other (the remainder: ticks spent on other
+        requests' set-up and on the host loop)."""
+        out = []
+        for lv in self.live.values():
+            if lv.finished_at is None:
+                continue
+            lat = lv.finished_at - lv.spec.arrival_s
+            queue = lv.admitted_at - lv.spec.arrival_s
+            other = lat - queue - lv.setup_s - lv.df_s - lv.wake_s
+            out.append({"id": lv.spec.id, "latency_s": lat, "queue_s": queue, "setup_s": lv.setup_s,
+                        "df_s": lv.df_s, "wake_s": lv.wake_s, "capture_s": lv.capture_s,
+                        "other_s": other, "ticks": lv.ticks, "points": lv.points,
+                        "n": lv.spec.n, "grid": lv.spec.grid, "mesh": lv.spec.mesh})
+        return out
+
     def summary(self, wall):
-        lat = np.array([lv.finished_at - lv.spec.arrival_s for lv in self.live.values()
-                        if lv.finished_at is not None])
+        br = self.latency_breakdown()
+        lat = np.array([b["latency_s"] for b in br])
         pts = sum(lv.points for lv in self.live.values())
-        return {"precision": self.precision, "requests": len(self.live),
-                "refused": len(self.sched.refused), "failed": len(self.sched.failed),
-                "ticks": self.ticks,
-                "wall_s": wall, "wake_points": int(pts),
-                "wake_points_per_s": pts / wall if wall > 0 else 0.0,
-                "wake_s": self.wake_s,
-                "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
-                "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
-                "mean_points_per_launch": float(np.mean(self.launch_points)) if self.launch_points else 0.0,
-                "graphs": len(self.wake.graphs), "graph_replays": self.wake.replays}
+        out = {"precision": self.precision, "requests": len(self.live),
+               "refused": len(self.sched.refused), "failed": len(self.sched.failed),
+               "ticks": self.ticks,
+               "wall_s": wall, "wake_points": int(pts),
+               "wake_points_per_s": pts / wall if wall > 0 else 0.0,
+               "wake_s": self.wake_s,
+               "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
+               "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
+               "mean_points_per_launch": float(np.mean(self.launch_points)) if self.launch_points else 0.0,
+               "graphs": len(self.wake.graphs), "graph_replays": self.wake.replays,
+               "graph_capture_s_in_stream": self.wake.capture_s,
+               "precapture_s": self.precapture_s}
+        if lat.size:
+            # the parts of the latency at the median and over the slowest 1 %
+            # (mean of each part over those requests)
+            order = np.argsort(lat)
+            tail = [br[i] for i in order[max(0, int(np.floor(0.99 * lat.size)) - 1):]]
+            mid = [br[i] for i in order[max(0, lat.size // 2 - 1):lat.size // 2 + 1]]
+            keys = ("latency_s", "queue_s", "setup_s", "df_s", "wake_s", "capture_s", "other_s")
+            out["breakdown_p50"] = {k: float(np.mean([b[k] for b in mid])) for k in keys}
+            out["breakdown_p99"] = {k: float(np.mean([b[k] for b in tail])) for k in keys}
+            out["breakdown_p99"]["requests"] = [{k: b[k] for k in ("id", "n", "grid", "mesh", "ticks")}
+                                                for b in tail]
+        return out
 
     def result(self, req_id):
         """[(step, dE_dct, x_kick)] of a served request."""
