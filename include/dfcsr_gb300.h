@@ -192,7 +192,8 @@ int dfcsr_grid_barrier_check(int blocks, int extra_arrivals, unsigned int max_sp
  * vx_x_fill is a DEVICE pointer to the fill value of vx_x (its mean).
  * ring64: [slot][nxi][nzi][5] doubles (or NULL); ring32: [slot][nxi][nzi][8]
  * floats (or NULL): fields 0..4, then in slot 5 the low part of density_x
- * (density_x - (double)(float)density_x), slots 6..7 zero.  Field order:
+ * (density_x - (double)(float)density_x), in slot 6 the low part of vx,
+ * slot 7 zero.  Field order:
  * density, density_x, density_z, vx, vx_x.  With ring64 the values follow
  * RegularGridInterpolator's term order exactly; with ring32 only, the
  * bilinear weights are applied as fused multiply-adds (the FP32 cells are

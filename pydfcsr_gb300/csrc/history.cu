@@ -68,15 +68,18 @@ __global__ void regrid5(const double *__restrict__ f0, const double *__restrict_
         for (int q = 0; q < 5; ++q) o[q] = v[q];
     }
     if (out32) {
-        // FP32 cell: density, density_x (high part), density_z, vx | vx_x,
-        // density_x low part (v - (double)hi), 0, 0.  density_x is carried as
-        // a float-float pair: its integral over x' cancels to ~1e-4 of its
-        // magnitude in the far region, so it needs ~48 bits.
+        // FP32 cell: density, density_x (high part), density_z, vx (high
+        // part) | vx_x, density_x low part (v - (double)hi), vx low part, 0.
+        // density_x and vx are carried as float-float pairs: the wake's
+        // density_x term sums to ~1/300 of its terms, and vx enters it through
+        // b - vx (..), where the two are of similar size after a bend.
         float4 *o = reinterpret_cast<float4 *>(out32 + (size_t)t * 8);
         const float hi = (float)v[1];
         const float lo = (float)(v[1] - (double)hi);
-        o[0] = make_float4((float)v[0], hi, (float)v[2], (float)v[3]);
-        o[1] = make_float4((float)v[4], lo, 0.f, 0.f);
+        const float vhi = (float)v[3];
+        const float vlo = (float)(v[3] - (double)vhi);
+        o[0] = make_float4((float)v[0], hi, (float)v[2], vhi);
+        o[1] = make_float4((float)v[4], lo, vlo, 0.f);
     }
 }
 

@@ -87,6 +87,16 @@ __device__ __forceinline__ double rho_at(const dfcsr_wake_job &J, double sp) {
     return r;
 }
 
+// One field of an FP32 ring cell as a double: density_x and vx are stored as
+// hi + lo (low parts in slots 5 and 6 of the 8-float cell).
+__device__ __forceinline__ double ring32_value(const float *ring32, size_t cell, int field) {
+    const float *c = ring32 + cell * 8;
+    double v = (double)c[field];
+    if (field == 1) v += (double)c[5];
+    else if (field == 3) v += (double)c[6];
+    return v;
+}
+
 __device__ __forceinline__ int ring_slot(const dfcsr_wake_job &J, int t) {
     int s = J.head + t;
     if (s >= J.cap) s -= J.cap;
@@ -105,7 +115,7 @@ __device__ inline double hist_field_fp64(const dfcsr_wake_job &J, int field, dou
     const int s0 = ring_slot(J, t0), s1 = ring_slot(J, t1);
     auto D = [&](int s, int xi, int zi) -> double {
         const size_t cell = ((size_t)s * J.nx + xi) * J.nz + zi;
-        return J.ring64 ? J.ring64[cell * 5 + field] : (double)J.ring32[cell * 8 + field];
+        return J.ring64 ? J.ring64[cell * 5 + field] : ring32_value(J.ring32, cell, field);
     };
     const double c00 = D(s0, x0, z0) * (1 - td) + D(s1, x0, z0) * td;
     const double c01 = D(s0, x0, z1) * (1 - td) + D(s1, x0, z1) * td;
@@ -140,7 +150,7 @@ __device__ __forceinline__ void gather5_fp64(const dfcsr_wake_job &J, double t, 
         double d[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k)
-            d[k] = J.ring64 ? J.ring64[c[k] * 5 + f] : (double)J.ring32[c[k] * 8 + f];
+            d[k] = J.ring64 ? J.ring64[c[k] * 5 + f] : ring32_value(J.ring32, c[k], f);
         const double c00 = d[0] * (1 - td) + d[1] * td;
         const double c01 = d[2] * (1 - td) + d[3] * td;
         const double c10 = d[4] * (1 - td) + d[5] * td;

@@ -59,10 +59,11 @@ constexpr int RW = 8;
 //  4: a = v.tau', b = v.n', e = tau'.n', h = |tau'|^2
 //  5: K1x - 1 = a g - 1 + b e, K2x = b g, K0z = a (1 - h), K1z = a e + b h
 //  6: K2z = b e, Q0 = R0.(n - n'), Q1 = n'.(n - n'), q2 = n.tau'
-//  7: M0 = Q0 - q2 r0, trapz weight in s', 0, 0
+//  7: M0 = Q0 - q2 r0, trapz weight in s', a - (float)a (a = word 4.x + this), 0
 //  8: 0, 0, 0, 0
 // row record words: x0 (int), x weight, u = x' - x'_ref (dw) | trapz weight in x',
-// x1 - x0 (int), x', 0
+// x1 - x0 (int), x', x weight - (float)x weight (the row's weight is shared by
+// every s' column, so density_x's x step uses it as a double-word)
 
 struct RegionMeta {
     int nxp, nsp, col_off, row_off;   // offsets in words within the point record
@@ -71,6 +72,11 @@ struct RegionMeta {
 struct PointMeta {
     int nreg, valid;
     float inv_dt_hi, inv_dt_lo, inv_dz_hi, inv_dz_lo;   // reciprocals of the history t and z steps (dw)
+    // per region: the trapz weights in the records are FP32 roundings of the
+    // s' and x' steps, the same relative rounding for every weight of the
+    // region (end weights are exactly half the inner ones); the region sum
+    // is multiplied by 1 + wdelta, the exact ratio of the FP64 steps to them
+    float wdelta[WAKE_MAX_REGIONS];
     RegionMeta reg[WAKE_MAX_REGIONS];
 };
 
@@ -128,7 +134,7 @@ __device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *
 // One history field at (slot, x, z) from the FP64 ring, else the FP32 ring.
 __device__ __forceinline__ double hist_cell(const dfcsr_wake_job &J, int field, int slot, int xi, int zi) {
     const size_t cell = ((size_t)slot * J.nx + xi) * J.nz + zi;
-    return J.ring64 ? J.ring64[cell * 5 + field] : (double)J.ring32[cell * 8 + field];
+    return J.ring64 ? J.ring64[cell * 5 + field] : ring32_value(J.ring32, cell, field);
 }
 
 struct alignas(16) GeoShared {
@@ -156,6 +162,7 @@ struct alignas(16) GeoShared {
     // FP32 per-region constants: trapz weights (end point, inner point) in
     // s' and x', curvature of the elements e_first + k, near band half-width
     float wsf[WAKE_MAX_REGIONS][2], wxf[WAKE_MAX_REGIONS][2];
+    float wdelta[WAKE_MAX_REGIONS];   // (step_s / wsf[r][1]) (step_x / wxf[r][1]) - 1
     float rhof[WAKE_MAX_REGIONS][GEO_MAXB + 1];
     float band_f;
     double inv_s, inv_x;        // reciprocals of the orbit-table and history x steps
@@ -242,7 +249,8 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
                        dw_float(dw_add(ae, dw_mul(bb, h))));
     o[6] = make_float4(dw_float(dw_mul(bb, e)), dw_float(Q0),
                        dw_float(dw_add(dw_mul(npx, nmx), dw_mul(npy, nmy))), dw_float(q2));
-    o[7] = make_float4(dw_float(dw_sub(Q0, dw_mul(q2, r0))), near ? 0.f : ws, 0.f, 0.f);   // band columns: FP64 kernel
+    o[7] = make_float4(dw_float(dw_sub(Q0, dw_mul(q2, r0))), near ? 0.f : ws,
+                       __fsub_rn(a.hi, dw_float(a)) + a.lo, 0.f);   // band columns: FP64 kernel
     o[8] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
@@ -258,17 +266,17 @@ __device__ __forceinline__ void row_dw(const dfcsr_wake_job &J, GeoShared &gs, i
     const bool in = (ux.hi > -1.f || (ux.hi == -1.f && ux.lo > 0.f)) &&
                     (ux.hi < fnx || (ux.hi == fnx && ux.lo < 0.f));
     int x0 = 0, x1 = 0;
-    float xw = 0.f;
+    dw xw{0.f, 0.f};
     if (in) {
         x0 = max((int)dw_floor(ux), 0);   // int() truncation: u in (-1, 0) -> 0
         x1 = (x0 == J.nx - 1) ? x0 : x0 + 1;
-        xw = dw_float(dw_add_f(ux, -(float)x0));
+        xw = dw_add_f(ux, -(float)x0);
     }
     const int n = gs.ax_x[r].n;
     const dw u = dw_sub(xpi, gs.xrefw[r]);
-    rb[2 * i] = make_float4(__int_as_float(x0), xw, u.hi, u.lo);
+    rb[2 * i] = make_float4(__int_as_float(x0), xw.hi, u.hi, u.lo);
     rb[2 * i + 1] = make_float4((i == 0 || i == n - 1) ? gs.wxf[r][0] : gs.wxf[r][1],
-                                __int_as_float(x1 - x0), dw_float(xpi), 0.f);
+                                __int_as_float(x1 - x0), dw_float(xpi), xw.lo);
     if (in) {
         atomicMin(&gs.lo[r], i);   // integer min / max: order independent
         atomicMax(&gs.hi[r], i);
@@ -354,7 +362,8 @@ __device__ __noinline__ void geometry_fp64(const dfcsr_wake_job &J, GeoShared &g
         o[5] = make_float4((float)((a * g - 1.0) + bb * e), (float)(bb * g), (float)(a * (1.0 - h)),
                            (float)(a * e + bb * h));
         o[6] = make_float4((float)(bb * e), (float)Q0, (float)(npx * nmx + npy * nmy), (float)q2);
-        o[7] = make_float4((float)(Q0 - q2 * r0), near ? 0.f : (float)ax_s.weight(j), 0.f, 0.f);   // band columns: FP64 kernel
+        o[7] = make_float4((float)(Q0 - q2 * r0), near ? 0.f : (float)ax_s.weight(j),
+                           (float)(a - (double)(float)a), 0.f);   // band columns: FP64 kernel
         o[8] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     // rows: x cell, offset, u = x' - x'_ref, x', trapz weight; valid row range
@@ -373,8 +382,9 @@ __device__ __noinline__ void geometry_fp64(const dfcsr_wake_job &J, GeoShared &g
         const bool in = axis_index(ux, J.nx, x0, x1, xw);
         float4 *rb = reinterpret_cast<float4 *>(prec + gs.rm[r].row_off);
         const dw u = dw_from(xpi - gs.xref[r]);
-        rb[2 * i] = make_float4(__int_as_float(x0), (float)xw, u.hi, u.lo);
-        rb[2 * i + 1] = make_float4((float)ax_x.weight(i), __int_as_float(x1 - x0), (float)xpi, 0.f);
+        const dw xwd = dw_from(xw);
+        rb[2 * i] = make_float4(__int_as_float(x0), xwd.hi, u.hi, u.lo);
+        rb[2 * i + 1] = make_float4((float)ax_x.weight(i), __int_as_float(x1 - x0), (float)xpi, xwd.lo);
         if (in) {
             atomicMin(&gs.lo[r], i);   // integer min / max: order independent
             atomicMax(&gs.hi[r], i);
@@ -579,6 +589,9 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
             gs.wsf[r][1] = A.n < 2 ? 0.f : (float)A.step;
             gs.wxf[r][0] = AX.n < 2 ? 0.f : (float)(0.5 * AX.step);
             gs.wxf[r][1] = AX.n < 2 ? 0.f : (float)AX.step;
+            gs.wdelta[r] = (A.n < 2 || AX.n < 2 || gs.wsf[r][1] == 0.f || gs.wxf[r][1] == 0.f)
+                               ? 0.f
+                               : (float)((A.step / (double)gs.wsf[r][1]) * (AX.step / (double)gs.wxf[r][1]) - 1.0);
         }
     }
     __syncthreads();
@@ -655,8 +668,10 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
         m.inv_dt_lo = gs.inv_t.lo;
         m.inv_dz_hi = gs.inv_z.hi;
         m.inv_dz_lo = gs.inv_z.lo;
-        for (int k = 0; k < WAKE_MAX_REGIONS; ++k)
+        for (int k = 0; k < WAKE_MAX_REGIONS; ++k) {
             m.reg[k] = (k < gs.nreg) ? gs.rm[k] : RegionMeta{0, 0, 0, 0};
+            m.wdelta[k] = (k < gs.nreg) ? gs.wdelta[k] : 0.f;
+        }
         meta[b] = m;
         obs_vx[b] = gs.vx_obs;
     }
@@ -696,61 +711,103 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
 // double-word value, so it agrees with the FP64 decision except within
 // ~1e-12 cells of a boundary (at u = -1 the reference's interpolant jumps
 // from an extrapolated value to zero).
-__device__ __forceinline__ bool axis_split_dw(int base, dw off, int n, int &i0, int &i1, float &w) {
+__device__ __forceinline__ bool axis_split_dw(int base, dw off, int n, int &i0, int &i1, float &w,
+                                              float &w_lo) {
     float k = floorf(off.hi);
-    float fr = __fadd_rn(__fsub_rn(off.hi, k), off.lo);   // off.hi - k is exact
-    if (fr < 0.f) { k = __fsub_rn(k, 1.f); fr = __fadd_rn(fr, 1.f); }
-    else if (fr >= 1.f) { k = __fadd_rn(k, 1.f); fr = __fsub_rn(fr, 1.f); }
+    dw fr = fast_two_sum(__fsub_rn(off.hi, k), off.lo);   // off.hi - k is exact
+    if (fr.hi < 0.f) { k = __fsub_rn(k, 1.f); fr = dw_add_f(fr, 1.f); }
+    else if (fr.hi >= 1.f) { k = __fadd_rn(k, 1.f); fr = dw_add_f(fr, -1.f); }
     const int ui = base + (int)k;
-    if (!(ui > -1 || (ui == -1 && fr > 0.f)) || ui >= n) return false;
-    if (ui == -1) { i0 = 0; w = __fsub_rn(fr, 1.f); }
-    else { i0 = ui; w = fr; }
+    if (!(ui > -1 || (ui == -1 && fr.hi > 0.f)) || ui >= n) return false;
+    if (ui == -1) { i0 = 0; fr = dw_add_f(fr, -1.f); }
+    else i0 = ui;
+    w = fr.hi;
+    w_lo = fr.lo;
     i1 = (i0 == n - 1) ? i0 : i0 + 1;
     return true;
 }
 
 struct Fields5 {
-    float den, dz, vx, vxx;
-    float dx_h, dx_d;   // density_x = dx_h + dx_d (offset form)
+    float den, dz, vxx;
+    dw dx, vx;   // double-word: interpolated in offset form, the t step in double-word
 };
 
-// A 32-byte history cell (den, dx_hi, dz, vx | vxx, dx_lo, pad, pad) in one
-// 256-bit non-coherent load; the two pad words are not kept.
-__device__ __forceinline__ void ld_cell(const float4 *p, float4 &a, float2 &b) {
-    float4 t;
+// A 32-byte history cell (den, dx_hi, dz, vx_hi | vxx, dx_lo, vx_lo, pad) in
+// one 256-bit non-coherent load; the pad word is not kept.
+__device__ __forceinline__ void ld_cell(const float4 *p, float4 &a, float4 &b) {
     asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
         : "l"(p));
-    b = make_float2(t.x, t.y);
 }
 
 // a + w (b - a) with one rounding for the product-add.
 __device__ __forceinline__ float lerp1(float a, float b, float w) { return fmaf(w, b - a, a); }
 
-// Trilinear FP32 gather of the five fields from ring32 [slot][nx][nz][8]
-// (cell: den, dx_hi, dz, vx | vxx, dx_lo, 0, 0), interpolating t, then x,
-// then z like the reference.  density_x (stored as hi + lo) comes back in
-// offset form: the corners enter as (hi_c - h) + lo_c with h the high part
-// of the first corner (the subtraction is exact for neighbouring values
-// within a factor 2), the trilinear chain runs on these small offsets and
-// the value is h + D, unrounded - the wake's density_x term is a sum that
-// cancels to ~1/300 of its terms, and this form keeps it to ~1e-9 of the
-// value instead of an FP32 rounding.
+// Bilinear (x, then z) interpolation of a hi + lo field in one history
+// slice, in offset form: the corners enter as (hi_c - h) + lo_c with h the
+// high part of the slice's first corner (the subtraction is exact for
+// neighbouring values within a factor 2, and neighbouring cells in x and z
+// differ by a few %), so the FP32 chain rounds only small numbers.  Returns
+// h and the interpolated offset D (value = h + D).
+__device__ __forceinline__ void slice_offset(float h00, float l00, float h01, float l01, float h10,
+                                             float l10, float h11, float l11, float xd, float zd,
+                                             float &h, float &D) {
+    h = h00;
+    const float o01 = __fadd_rn(__fsub_rn(h01, h), l01);
+    const float o10 = __fadd_rn(__fsub_rn(h10, h), l10);
+    const float o11 = __fadd_rn(__fsub_rn(h11, h), l11);
+    const float e0 = lerp1(l00, o10, xd);
+    const float e1 = lerp1(o01, o11, xd);
+    D = lerp1(e0, e1, zd);
+}
+
+// P0 + td (P1 - P0) with P = h + D per slice, in double-word: consecutive
+// history slices differ by up to ~100 % (a beam step apart), so this step is
+// the one an FP32 chain would round at the value's own size.
+__device__ __forceinline__ dw tlerp_dw(float h0, float D0, float h1, float D1, float td) {
+    const dw dh = two_sum(h1, -h0);
+    const dw d = fast_two_sum(dh.hi, __fadd_rn(dh.lo, __fsub_rn(D1, D0)));
+    const dw p = two_prod(td, d.hi);
+    const dw a = two_sum(h0, p.hi);
+    return fast_two_sum(a.hi, __fadd_rn(__fadd_rn(a.lo, D0), __fmaf_rn(td, d.lo, p.lo)));
+}
+
+// a + w (b - a) for double-words a, b (hi + lo, not renormalised between
+// steps) and a double-word weight wh + wl: the difference and the product
+// are formed without error (TwoSum, FMA TwoProd), so the result carries
+// ~2^-46 of the values' magnitude instead of an FP32 rounding.  Each weight
+// of a gather is shared by many terms of the wake's sums (the x weight by
+// every s' column of a row), so it must not be rounded to FP32 either.
+__device__ __forceinline__ dw lerp_dw2(dw a, dw b, float wh, float wl) {
+    const dw s = two_sum(b.hi, -a.hi);
+    const float dl = __fadd_rn(s.lo, __fsub_rn(b.lo, a.lo));
+    const dw p = two_prod(wh, s.hi);
+    const dw r = two_sum(a.hi, p.hi);
+    const float pl = __fmaf_rn(wl, s.hi, __fmaf_rn(wh, dl, p.lo));
+    return dw{r.hi, __fadd_rn(__fadd_rn(r.lo, a.lo), pl)};
+}
+
+// Trilinear gather of the five fields from ring32 [slot][nx][nz][8] at
+// (t, x, z): density, density_z and vx_x in FP32 (t, then x, then z, like
+// the reference); density_x as a double-word lerp chain and vx in per-slice
+// offset form with a double-word t step (the wake's density_x term cancels
+// to ~1/300 of its terms, and vx enters it through b - vx (K1x + vx K2x)
+// where the two are of similar size after a bend).
 // c<x><t>: float4 index of the z0 cell at x0/x1, t0/t1; dzc: float4 step to z1.
 __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint32_t c00, uint32_t c01,
-                                           uint32_t c10, uint32_t c11, uint32_t dzc, float td, float xd,
-                                           float zd) {
+                                           uint32_t c10, uint32_t c11, uint32_t dzc, float td,
+                                           float td_lo, float xd, float xd_lo, float zd, float zd_lo) {
     // one 32-byte load per cell (the cells are 32-byte aligned)
     float4 A0, A1, B0, B1, C0, C1, D0, D1;
-    float2 a0, a1, b0, b1, c0, c1, d0, d1;
-    ld_cell(ring + c00, A0, a0);
-    ld_cell(ring + c00 + dzc, A1, a1);
-    ld_cell(ring + c01, B0, b0);
-    ld_cell(ring + c01 + dzc, B1, b1);
-    ld_cell(ring + c10, C0, c0);
-    ld_cell(ring + c10 + dzc, C1, c1);
-    ld_cell(ring + c11, D0, d0);
-    ld_cell(ring + c11 + dzc, D1, d1);
+    float4 a0, a1, b0, b1, c0, c1, d0, d1;
+    ld_cell(ring + c00, A0, a0);   // t0 x0 z0
+    ld_cell(ring + c00 + dzc, A1, a1);   // t0 x0 z1
+    ld_cell(ring + c01, B0, b0);   // t1 x0 z0
+    ld_cell(ring + c01 + dzc, B1, b1);   // t1 x0 z1
+    ld_cell(ring + c10, C0, c0);   // t0 x1 z0
+    ld_cell(ring + c10 + dzc, C1, c1);   // t0 x1 z1
+    ld_cell(ring + c11, D0, d0);   // t1 x1 z0
+    ld_cell(ring + c11 + dzc, D1, d1);   // t1 x1 z1
     auto tri = [&](float v00a, float v00b, float v01a, float v01b, float v10a, float v10b,
                    float v11a, float v11b) -> float {
         const float c00_ = lerp1(v00a, v00b, td);
@@ -764,14 +821,24 @@ __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint
     Fields5 r;
     r.den = tri(A0.x, B0.x, A1.x, B1.x, C0.x, D0.x, C1.x, D1.x);
     r.dz = tri(A0.z, B0.z, A1.z, B1.z, C0.z, D0.z, C1.z, D1.z);
-    r.vx = tri(A0.w, B0.w, A1.w, B1.w, C0.w, D0.w, C1.w, D1.w);
     r.vxx = tri(a0.x, b0.x, a1.x, b1.x, c0.x, d0.x, c1.x, d1.x);
-    const float h = A0.y;
-    r.dx_h = h;
-    r.dx_d = tri(a0.y, __fadd_rn(__fsub_rn(B0.y, h), b0.y), __fadd_rn(__fsub_rn(A1.y, h), a1.y),
-                 __fadd_rn(__fsub_rn(B1.y, h), b1.y), __fadd_rn(__fsub_rn(C0.y, h), c0.y),
-                 __fadd_rn(__fsub_rn(D0.y, h), d0.y), __fadd_rn(__fsub_rn(C1.y, h), c1.y),
-                 __fadd_rn(__fsub_rn(D1.y, h), d1.y));
+    float h0, q0, h1, q1;
+    // density_x (high parts in .y of the first float4, low parts in .y of
+    // the second): the reference's t, x, z lerp chain in double-word
+    {
+        const dw c00 = lerp_dw2(dw{A0.y, a0.y}, dw{B0.y, b0.y}, td, td_lo);
+        const dw c01 = lerp_dw2(dw{A1.y, a1.y}, dw{B1.y, b1.y}, td, td_lo);
+        const dw c10 = lerp_dw2(dw{C0.y, c0.y}, dw{D0.y, d0.y}, td, td_lo);
+        const dw c11 = lerp_dw2(dw{C1.y, c1.y}, dw{D1.y, d1.y}, td, td_lo);
+        const dw e0 = lerp_dw2(c00, c10, xd, xd_lo);
+        const dw e1 = lerp_dw2(c01, c11, xd, xd_lo);
+        const dw v = lerp_dw2(e0, e1, zd, zd_lo);
+        r.dx = fast_two_sum(v.hi, v.lo);
+    }
+    // vx: high parts in .w of the first float4, low parts in .z of the second
+    slice_offset(A0.w, a0.z, A1.w, a1.z, C0.w, c0.z, C1.w, c1.z, xd, zd, h0, q0);
+    slice_offset(B0.w, b0.z, B1.w, b1.z, D0.w, d0.z, D1.w, d1.z, xd, zd, h1, q1);
+    r.vx = tlerp_dw(h0, q0, h1, q1, td);
     return r;
 }
 
@@ -901,8 +968,9 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
             const dw ot = dw_add_f(toff, -__fmul_rn(delf, V.inv_dt.hi));
             const dw oz = dw_add_abs(zoff, dw_mul(del, V.inv_dz));
             int t0, t1, z0, z1;
-            float td, zd;
-            if (!axis_split_dw(tcell, ot, V.nt, t0, t1, td) || !axis_split_dw(zcell, oz, V.nz, z0, z1, zd))
+            float td, zd, td_lo, zd_lo;
+            if (!axis_split_dw(tcell, ot, V.nt, t0, t1, td, td_lo) ||
+                !axis_split_dw(zcell, oz, V.nz, z0, z1, zd, zd_lo))
                 continue;   // every field is zero outside the history grid
             // x: rows outside the history grid are not in [i_lo, i_hi)
             const int x0 = __float_as_int(ra.x);
@@ -914,30 +982,31 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
             const uint32_t c1x0 = ((uint32_t)s1 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
             const uint32_t dxc = (uint32_t)__float_as_int(rw.y) * nzc;
             const Fields5 F = gather5(V.ring, c0x0, c1x0, c0x0 + dxc, c1x0 + dxc,
-                                      2u * (uint32_t)(z1 - z0), td, xd, zd);
-            const float vr = F.vx;
+                                      2u * (uint32_t)(z1 - z0), td, td_lo, xd, rw.w, zd, zd_lo);
+            const float vr = F.vx.hi;
             const float4 q4 = cr[4], q5 = cr[5];
             // density_x term: w scale brx dx / |r - r'| in double-word, with
-            // brx = K0x - vr (K1x + vr K2x) and scale = 1 + x' rho
+            // brx = K0x - vx (K1x + vx K2x) and scale = 1 + x' rho
             const float dsc = __fmul_rn(rw.z, rho);
-            const float db = -vr * fmaf(vr, q5.y, q5.x + 1.f);
-            dw A = dw_add_f(K0x, db);
+            dw A = dw_sub_abs(K0x, dw_mul_f(F.vx, fmaf(vr, q5.y, q5.x + 1.f)));
             A = dw_add_f(A, __fmul_rn(dsc, A.hi));
             const dw w = two_prod(wx, ws);
-            const dw dxv = two_sum(F.dx_h, F.dx_d);
-            const dw T = dw_mul(dw_mul(dw_mul(A, w), dxv), dw_recip_from(rd, inv_r));
-            acc.zx = dw_add_abs(acc.zx, T);
-            // the rest of the longitudinal integrand (FP32)
+            const dw wr = dw_mul(w, dw_recip_from(rd, inv_r));     // w / |r - r'|
+            acc.zx = dw_add_abs(acc.zx, dw_mul(dw_mul(A, F.dx), wr));
+            // density term -scale (a + vx b) den vx_x w / |r - r'| in double-word
             const float4 q6 = cr[6];
             const float scale = 1.f + dsc;
+            const dw p1w = dw_add_f(dw{q4.x, q7.z}, __fmul_rn(vr, q4.y));
+            dw Dn = dw_neg(dw_mul(two_prod(F.den, F.vxx), p1w));
+            Dn = dw_add_f(Dn, __fmul_rn(dsc, Dn.hi));
+            acc.zx = dw_add_abs(acc.zx, dw_mul(Dn, wr));
+            // density_z term (FP32)
             const float wf = wx * ws;
             const float brz = q5.z - vr * fmaf(vr, q6.x, q5.w);
-            const float p1 = fmaf(vr, q4.y, q4.x);
-            const float rest = (F.dz * brz - scale * p1 * F.den * F.vxx) * inv_r;
-            kahan(acc.sz, acc.cz, wf * rest);
+            kahan(acc.sz, acc.cz, wf * (F.dz * brz * inv_r));
             // transverse integrand (FP32)
             const float uf = uu.hi;
-            const float dxf = dw_float(dxv);
+            const float dxf = dw_float(F.dx);
             const float q1x = q6.y - uf * q6.z;
             const float M = q7.x - uf * q6.z - q6.w * delf;
             const float e = q4.z;
@@ -951,7 +1020,10 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
 
 // Persistent: CTAs take points of the batch from a work counter.  Writes the
 // FP64 region sums part[b][r][2].
-__global__ void __launch_bounds__(MX_THREADS, 3)
+#ifndef MX_INTEGRAL_BLOCKS
+#define MX_INTEGRAL_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(MX_THREADS, MX_INTEGRAL_BLOCKS)
 mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
                int64_t first, int64_t count, size_t rec_words, const float *__restrict__ rec,
                const PointMeta *__restrict__ meta, const int2 *__restrict__ rows_valid,
@@ -1003,8 +1075,10 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
                 }
             }
             if (tid == 0) {
-                part[((size_t)b * WAKE_MAX_REGIONS + r) * 2 + 0] = dw_to_double(reg_z);
-                part[((size_t)b * WAKE_MAX_REGIONS + r) * 2 + 1] = dw_to_double(reg_x);
+                const double wd = (double)m->wdelta[r];
+                const double vz = dw_to_double(reg_z), vx = dw_to_double(reg_x);
+                part[((size_t)b * WAKE_MAX_REGIONS + r) * 2 + 0] = fma(vz, wd, vz);
+                part[((size_t)b * WAKE_MAX_REGIONS + r) * 2 + 1] = fma(vx, wd, vx);
             }
         }
         __syncthreads();
