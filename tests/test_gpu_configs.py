@@ -6,10 +6,15 @@
   1e-10, the wake at sampled mesh points 1e-8 (relative, FP64 drop-in).
 * chicane with the double-horn beam (4e6 particles, 384^2, 96^2 mesh) and the
   large beam (1e7 particles, 512^2, 128^2 mesh): the mixed-precision wake
-  against the plain FP64 kernel on the full mesh (max_rel and rms_rel <=
-  1e-4, S = peak |wake| over both components), with and without the FP64
-  near-source band, and bitwise repeatability.  The FP64 kernel itself is
-  checked against the oracle above and in test_gpu_parity.
+  against the plain FP64 kernel on the full mesh, with and without the FP64
+  near-source band, and bitwise repeatability; the large beam also in the
+  drift after the third bend, where the wake is ~1/300 of its size in the
+  bends while the history's terms are not.
+* the chicane benchmark beam (2e6 particles, 256^2, 64^2 mesh) over the
+  whole 100-step run, every 5th step.
+Gates: max_rel, rms_rel and the pointwise error max|a-b| / max(|b|, 1e-3 S)
+(S = peak |wake| over both components) all <= 1e-4.  The FP64 kernel itself
+is checked against the oracle above and in test_gpu_parity.
 """
 import numpy as np
 import pytest
@@ -77,7 +82,7 @@ def _mixed_vs_fp64(name, steps, check_at, near_band=0.0):
     from pydfcsr_gb300.synthetic import workload
     wl = workload(name)
     run = WakeRun(wl.lattice, wl.beam(), wl.deposit, wl.integration, wl.mesh, precision="both",
-                  grid_rule="configured", host_transport=True)
+                  grid_rule="configured", host_transport=False)
     out = []
     for k in range(1, steps + 1):
         run.step(k)
@@ -106,16 +111,29 @@ def test_double_horn_full_size_mixed_vs_fp64():
     assert out[0][1] < 1.0 < out[-1][1]
     for k, slope, res in out:
         e = res[0.0]
-        assert e["max_rel"] <= 1e-4 and e["rms_rel"] <= 1e-4, (k, slope, e)
+        assert max(e.values()) <= 1e-4, (k, slope, e)
 
 
 @cuda
 def test_large_beam_full_size_mixed_vs_fp64_with_band():
     from pydfcsr_gb300.synthetic import workload
     sz = 30e-6
-    out = _mixed_vs_fp64("chicane_c5", 120, (10, 120), near_band=20 * sz)
+    out = _mixed_vs_fp64("chicane_c5", 230, (10, 120, 230), near_band=20 * sz)
     assert workload("chicane_c5").n_particles == 10_000_000
-    assert out[0][1] < 1.0 < out[-1][1]
+    assert out[0][1] < 1.0 < out[1][1] and out[2][1] > 1.0
     for k, slope, res in out:
         for band, e in res.items():
-            assert e["max_rel"] <= 1e-4 and e["rms_rel"] <= 1e-4, (k, band, e)
+            assert max(e.values()) <= 1e-4, (k, band, e)
+
+
+@cuda
+def test_chicane_whole_run_mixed_vs_fp64():
+    """The benchmark's chicane beam over all 100 steps (both branches of
+    get_CSR_wake, the first steps with two or three history slices), every
+    5th step and the first two."""
+    steps = (1, 2) + tuple(range(5, 101, 5))
+    out = _mixed_vs_fp64("chicane_c2", 100, steps)
+    assert any(slope > 1.0 for _, slope, _ in out) and any(slope < 1.0 for _, slope, _ in out)
+    for k, slope, res in out:
+        e = res[0.0]
+        assert max(e.values()) <= 1e-4, (k, slope, e)

@@ -202,11 +202,11 @@ def test_wake_fp64_golden(tag):
         csr.calculate_2D_CSR("fp64")
         assert rel_err(csr.dE_dct, g["mesh_dE"]) < 1e-9
         assert rel_err(csr.x_kick, g["mesh_xkick"]) < 1e-9
-        # mixed precision on the same history: <= 1e-4
+        # mixed precision on the same history: max_rel, rms_rel and the
+        # pointwise error (floor 1e-3 of the peak) all <= 1e-4
         csr.calculate_2D_CSR("mixed")
         e = wake_errors(csr.dE_dct, csr.x_kick, g["mesh_dE"], g["mesh_xkick"])
-        assert e["max_rel"] < 1e-4 and e["rms_rel"] < 1e-4, e
-        assert e["pointwise_dE"] < 1e-2 and e["pointwise_xk"] < 1e-2, e
+        assert max(e.values()) <= 1e-4, e
 
 
 @cuda
@@ -233,7 +233,7 @@ def test_wake_mixed_geometry_paths(tag):
         out[path] = (dE.cpu().numpy(), xk.cpu().numpy())
     for path, (dE, xk) in out.items():
         e = wake_errors(dE, xk, g["mesh_dE"], g["mesh_xkick"])
-        assert e["max_rel"] < 1e-4 and e["rms_rel"] < 1e-4, (path, e)
+        assert max(e.values()) <= 1e-4, (path, e)
     e = wake_errors(*out["fp64"], *out["dw"])
     assert e["max_rel"] < 1e-6, e
 
@@ -311,8 +311,7 @@ def test_wake_chicane_mixed_vs_oracle():
     assert rel_err(dE64.ravel(), ref[0]) < 1e-8
     assert rel_err(xk64.ravel(), ref[1]) < 1e-8
     e = wake_errors(dE32, xk32, ref[0], ref[1])
-    assert e["max_rel"] < 1e-4 and e["rms_rel"] < 1e-4, e
-    assert e["pointwise_dE"] < 1e-2 and e["pointwise_xk"] < 1e-2, e
+    assert max(e.values()) <= 1e-4, e
 
 
 @cuda
