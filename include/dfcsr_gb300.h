@@ -294,15 +294,21 @@ int dfcsr_wake_integrand(const dfcsr_wake_job *job, double s, double x,
                          const double *sp, const double *xp, int64_t m, int ignore_vx,
                          double *Iz, double *Ix, void *stream);
 
-/* Mixed precision: FP64 per-(point, s') retarded geometry written as
- * per-column records, FP32 gathers and integrand with history coordinates
- * carried as integer cell + FP32 offset, Kahan-compensated FP32 sums reduced
- * in FP64 (fixed order).  Needs ring32 in every job (below 64 GiB: cells are
- * addressed with 32-bit offsets).  xbins_max / zbins_max
+/* Mixed precision: the per-(point, s') retarded geometry (FP64, or
+ * double-word FP32 from the job's double-word orbit tables) written as
+ * per-column records; per integrand point the distance, the retarded shift
+ * and the history coordinates in double-word FP32; FP32 gathers from ring32
+ * with density_x and vx (stored hi + lo) interpolated in double-word; the
+ * density_x and density terms of the longitudinal integrand summed in
+ * double-word, the rest Kahan-compensated FP32; fixed-order block sums,
+ * region sums in FP64.  Max, rms and pointwise error vs the FP64 kernel on
+ * the same history <= 2e-5 of the peak on the benchmark workloads.  Needs
+ * ring32 in every job (below 64 GiB: cells are addressed with 32-bit
+ * offsets).  xbins_max / zbins_max
  * bound the integration bins of all jobs in the call.  use_band != 0 runs
  * the s' columns with |s' - s| < job.near_band through the FP64 integrand.
  * Scratch: dfcsr_wake_workspace_bytes(xbins_max, zbins_max, n); points are
- * processed in batches of up to 1 GiB of per-point records (~61 KB per
+ * processed in batches of up to 1 GiB of per-point records (~74 KB per
  * point at 100 x 100 bins: a 64^2 mesh is one batch). */
 size_t dfcsr_wake_workspace_bytes(int xbins_max, int zbins_max, int64_t n);
 int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_of_point,

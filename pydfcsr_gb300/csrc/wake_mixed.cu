@@ -794,6 +794,7 @@ __device__ __forceinline__ dw lerp_dw2(dw a, dw b, float wh, float wl) {
 // to ~1/300 of its terms, and vx enters it through b - vx (K1x + vx K2x)
 // where the two are of similar size after a bend).
 // c<x><t>: float4 index of the z0 cell at x0/x1, t0/t1; dzc: float4 step to z1.
+template <bool DXDW>
 __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint32_t c00, uint32_t c01,
                                            uint32_t c10, uint32_t c11, uint32_t dzc, float td,
                                            float td_lo, float xd, float xd_lo, float zd, float zd_lo) {
@@ -824,8 +825,18 @@ __device__ __forceinline__ Fields5 gather5(const float4 *__restrict__ ring, uint
     r.vxx = tri(a0.x, b0.x, a1.x, b1.x, c0.x, d0.x, c1.x, d1.x);
     float h0, q0, h1, q1;
     // density_x (high parts in .y of the first float4, low parts in .y of
-    // the second): the reference's t, x, z lerp chain in double-word
-    {
+    // the second): the reference's t, x, z lerp chain in double-word where
+    // its terms cancel (DXDW: the far and middle regions); near the source
+    // they do not, and the corners enter in offset form from the first
+    // corner's high part, (hi_c - h) + lo_c, with an FP32 chain
+    if (!DXDW) {
+        const float h = A0.y;
+        const float D = tri(a0.y, __fadd_rn(__fsub_rn(B0.y, h), b0.y), __fadd_rn(__fsub_rn(A1.y, h), a1.y),
+                            __fadd_rn(__fsub_rn(B1.y, h), b1.y), __fadd_rn(__fsub_rn(C0.y, h), c0.y),
+                            __fadd_rn(__fsub_rn(D0.y, h), d0.y), __fadd_rn(__fsub_rn(C1.y, h), c1.y),
+                            __fadd_rn(__fsub_rn(D1.y, h), d1.y));
+        r.dx = two_sum(h, D);
+    } else {
         const dw c00 = lerp_dw2(dw{A0.y, a0.y}, dw{B0.y, b0.y}, td, td_lo);
         const dw c01 = lerp_dw2(dw{A1.y, a1.y}, dw{B1.y, b1.y}, td, td_lo);
         const dw c10 = lerp_dw2(dw{C0.y, c0.y}, dw{D0.y, d0.y}, td, td_lo);
@@ -921,6 +932,7 @@ struct ChunkSums {
 // product chain w scale brx dx / |r - r'|.  The other terms are FP32.
 constexpr int MX_ROWBLK = 4;
 
+template <bool DXDW>
 __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float4 *__restrict__ rows,
                                              const RingView &V, int i_lo, int i_hi, int C, ChunkSums &acc) {
     const int nblk = (i_hi - i_lo + MX_ROWBLK - 1) / MX_ROWBLK;
@@ -981,7 +993,7 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
             const uint32_t c0x0 = ((uint32_t)s0 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
             const uint32_t c1x0 = ((uint32_t)s1 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
             const uint32_t dxc = (uint32_t)__float_as_int(rw.y) * nzc;
-            const Fields5 F = gather5(V.ring, c0x0, c1x0, c0x0 + dxc, c1x0 + dxc,
+            const Fields5 F = gather5<DXDW>(V.ring, c0x0, c1x0, c0x0 + dxc, c1x0 + dxc,
                                       2u * (uint32_t)(z1 - z0), td, td_lo, xd, rw.w, zd, zd_lo);
             const float vr = F.vx.hi;
             const float4 q4 = cr[4], q5 = cr[5];
@@ -1066,7 +1078,12 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
                     for (int k = tid; k < C * (CW / 4); k += blockDim.x) sm.col[k] = cb[k];
                     __syncthreads();
                     ChunkSums acc{dw{0.f, 0.f}, 0.f, 0.f, 0.f, 0.f};
-                    chunk_points(sm, rows, V, rv.x, rv.y, C, acc);
+                    // regions 0 and 1 (far and middle): density_x's terms
+                    // cancel to ~1/300 of their size there
+                    if (r < 2)
+                        chunk_points<true>(sm, rows, V, rv.x, rv.y, C, acc);
+                    else
+                        chunk_points<false>(sm, rows, V, rv.x, rv.y, C, acc);
                     // Kahan state s - c exactly as a double-word
                     dw bz = dw_add(acc.zx, two_sum(acc.sz, -acc.cz)), bx = two_sum(acc.sx, -acc.cx);
                     block_sum2_dw(bz, bx, sm.red);
