@@ -574,7 +574,7 @@ def gpu_arm(a):
     # the history up to the window (untimed), then W warm-up steps; the side
     # stream carries the next step's moments and deposit
     side = torch.cuda.Stream()
-    timed_steps(run, sets, 1, first - W - 1, a.precision, side=side)
+    timed_steps(run, sets, 1, first - W - 1, a.precision, wake=False, side=side)
     timed_steps(run, sets, first - W, W, a.precision, side=side)
     barrier()
     fma_peaks = measure_fma_peaks()
@@ -666,7 +666,7 @@ def gpu_arm(a):
     if not a.no_e2e:
         re2e, _ = make_run(wl, lattice, a.precision, seed_offset=beam_seed(rank))
         sets = device_step_sets(re2e, last)
-        timed_steps(re2e, sets, 1, first - W - 1, a.precision, side=side)   # history (untimed)
+        timed_steps(re2e, sets, 1, first - W - 1, a.precision, wake=False, side=side)   # history
         host_sets = []
         for t in sets[first - W - 1:last]:
             h = torch.empty((3, t.shape[1]), dtype=torch.float64, pin_memory=True)
@@ -832,11 +832,17 @@ def roofline(kname, launch_ms, launches, K, npts, wl, run, fma_peaks, hbm, preci
             "peak_source": "measured FP64 FMA rate of this GPU (peaks_measured)"}
 
 
-# From an ncu capture of wake_mixed_integral on this workload (profiles/):
-# FP32 operations and DRAM bytes per integrand point, and the binding unit.
-INTEGRAL_FLOPS_PER_POINT = 150
-INTEGRAL_DRAM_BYTES_PER_POINT = 1.0
-INTEGRAL_BINDING = "to be measured"
+# From an ncu capture of wake_mixed_integral on this workload at a 4-region
+# step (profiles/wake_mixed_integral_chicane.md): FP32 operations per
+# integrand point (207.0 M FFMA x 2 + 938.2 M FADD/FMUL warp instructions x
+# 32 lanes / 2.048e8 points), DRAM bytes per integrand point (376.5 + 38.6
+# MB / 2.048e8), and the binding unit.
+INTEGRAL_FLOPS_PER_POINT = 211
+INTEGRAL_DRAM_BYTES_PER_POINT = 2.03
+INTEGRAL_BINDING = ("latency of the history gathers at 24 warps per SM (long-scoreboard stalls "
+                    "3.6 per issued instruction; issue 61 %, FMA pipe 47 %, L1TEX 67 %, L1 hits "
+                    "21 %, L2 hits 95 %); the FP32 mix is mostly FADD (double-word arithmetic), "
+                    "so the FMA-rate peak overstates what the pipe can reach")
 
 
 def stage_rooflines(kt, K, wl, run, hbm, fma_peaks):
