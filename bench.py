@@ -857,18 +857,28 @@ def stage_rooflines(kt, K, wl, run, hbm, fma_peaks):
     npts = wl.mesh["xbins"] * wl.mesh["zbins"]
     ip = wl.integration
     rec = (4 * ip["zbins"] * 144 + 5 * ip["xbins"] * 32)   # record bytes written per point (bound)
+    # (algorithmic bytes per step, FP64 operations per step or None, what
+    # the bytes are, the unit that binds the stage per its ncu profile)
     algo = {
-        "beam_moments": (32.0 * n, "hbm", "2 passes x (x, z) FP64 = 32 B per particle"),
-        "deposit_cic2d": (24.0 * n + 16.0 * cells, "hbm",
-                          "x, z, px read once (24 B per particle) + 2 grids written"),
-        "df_finalize": (7 * 8.0 * cells, "hbm", "2 fields read + 5 written, 8 B per cell"),
-        "history_regrid": (32.0 * nxi * nzi + 40.0 * cells, "hbm",
-                           "one FP32 ring slot written (32 B per cell) + 5 source fields read"),
-        "wake_mixed_geometry": (float(npts * rec), "hbm",
-                                "per-point column and row records written (bound)"),
+        "beam_moments": (32.0 * n, 15.0 * n, "2 passes x (x, z) FP64 = 32 B per particle; 15 FP64 "
+                         "operations per particle (shifted sums)", "FP64 pipe"),
+        "deposit_cic2d": (24.0 * n + 16.0 * cells, 20.0 * n,
+                          "x, z, px read once (24 B per particle) + 2 grids written; 20 FP64 "
+                          "operations per particle (cell keys 6, per-cell moment sums 14)",
+                          "FP64 pipe (moment sums) and the latency of the sort passes"),
+        "df_finalize": (7 * 8.0 * cells, None, "2 fields read + 5 written, 8 B per cell",
+                        "latency of nine dependent phases (grid barriers, FP64 reductions) over "
+                        "a grid of ~65k cells"),
+        "history_regrid": (32.0 * nxi * nzi + 40.0 * cells, 40.0 * nxi * nzi,
+                           "one FP32 ring slot written (32 B per cell) + 5 source fields read; "
+                           "5 fields x 4 corners x 2 FP64 operations per target cell",
+                           "FP64 latency"),
+        "wake_mixed_geometry": (float(npts * rec), None,
+                                "per-point column and row records written (bound)",
+                                "issue (double-word FP32 arithmetic)"),
     }
     out = {}
-    for name, (work, bound, how) in algo.items():
+    for name, (work, fp64, how, binding) in algo.items():
         ms, launches = kt.get(name, (0.0, 0))
         if not launches:
             continue
@@ -877,7 +887,11 @@ def stage_rooflines(kt, K, wl, run, hbm, fma_peaks):
         gbs = per_launch_work / (per_launch_ms * 1e-3) / 1e9
         out[name] = {"ms_per_step": ms / K, "launches_per_step": launches / K,
                      "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
-                     "bound": bound, "algorithmic": how}
+                     "bound": "hbm", "algorithmic": how, "binding": binding}
+        if fp64 is not None:
+            tf = fp64 * K / launches / (per_launch_ms * 1e-3) / 1e12
+            out[name]["fp64"] = {"achieved_tflops": tf, "peak_tflops": fma_peaks["fp64_tflops"],
+                                 "frac": tf / fma_peaks["fp64_tflops"]}
     return out
 
 
