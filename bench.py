@@ -341,6 +341,9 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True, side
             csr.get_CSR_mesh()
             s, x = csr.mesh_device()
             run.last = csr.wake_device(s, x, precision)
+            # get_CSR_wake's branch at this step: 4 regions when |slope| > 1
+            run.branch_log = getattr(run, "branch_log", {})
+            run.branch_log[k] = abs(float(beam._slope[0])) > 1
         if k + 2 <= last:
             st[k + 2] = status(k + 2)
         if events is not None:
@@ -348,17 +351,23 @@ def timed_steps(run, sets, first, count, precision, events=None, wake=True, side
             events.append(ev)
 
 
-def tracking_steps(run, first, count, precision, step_size):
+def tracking_steps(run, first, count, precision, step_size, early_deposit=True):
     """The reference's run loop with the CSR kick applied (CSR.py:297-334):
     transport by the step's matrix and beam statistics, the DF step, the wake
     on the mesh, Beam.apply_wakes (pz and px kicks) - every step depends on
-    the previous wake, so nothing overlaps across steps."""
+    the previous wake, so nothing overlaps across steps.  With
+    ``early_deposit`` the deposit is enqueued right behind the moments, on
+    the grid taken from the device moments, before the host waits for their
+    copy (the GPU deposits while the host sizes the rest of the step)."""
     from pydfcsr_gb300.runtime import as_device_f64
     csr, beam = run.csr, run.beam
     for k in range(first, first + count):
-        beam.track(run.plan.matrix(k), 0.0)
+        beam.track(run.plan.matrix(k), 0.0, wait=not early_deposit)
+        dep = None
+        if early_deposit:
+            dep = csr.DF_tracker.deposit_DF(beam.x, beam.z, beam.px, beam.moments_device)
         beam.position = float(run.plan.positions[k])
-        csr.update_history(run.plan.formation_length(k, beam.sigma_z))
+        csr.update_history(run.plan.formation_length(k, beam.sigma_z), deposited=dep)
         csr.get_CSR_mesh()
         s, x = csr.mesh_device()
         dE, xk = csr.wake_device(s, x, precision)
@@ -625,8 +634,10 @@ def gpu_arm(a):
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     if k_n:
-        out["roofline"] = roofline(kname, k_ms / k_n, k_n, K, npts, wl, run, fma_peaks, hbm,
-                                   a.precision)
+        n_sms = torch.cuda.get_device_properties(local).multi_processor_count
+        out["roofline"] = roofline(kname, k_ms / k_n, k_n,
+                                   integrand_points(wl, run, range(first, last + 1)), npts,
+                                   fma_peaks, hbm, a.precision, ck.get("sm_mhz"), n_sms)
     out["stages"] = stage_rooflines(kt, K, wl, run, hbm, fma_peaks)
     out["peaks_measured"] = fma_peaks
     out["gpu_launches"] = int(n_launch)   # this library's kernel launches in the timed region
@@ -800,12 +811,20 @@ def other_workloads(W, K, side, accuracy):
     return out
 
 
-def roofline(kname, launch_ms, launches, K, npts, wl, run, fma_peaks, hbm, precision):
-    """Roofline object of the dominant kernel (see ROOFLINE_NOTE)."""
+def integrand_points(wl, run, steps):
+    """Integrand points of the wake over ``steps`` per observation point:
+    4 x xbins x zbins in the 3-region branch of get_CSR_wake, 5 x in the
+    4-region one (the branch of each step as timed_steps logged it)."""
     ip = wl.integration
-    slope = abs(run.beam._slope[0])
-    per_obs = (5 if slope > 1 else 4) * ip["xbins"] * ip["zbins"]
-    pts = npts * per_obs * K / launches          # integrand points per launch
+    per = ip["xbins"] * ip["zbins"]
+    return sum((5 if run.branch_log[k] else 4) * per for k in steps)
+
+
+def roofline(kname, launch_ms, launches, per_obs_total, npts, fma_peaks, hbm, precision, clock_mhz,
+             n_sms):
+    """Roofline object of the dominant kernel: ``per_obs_total`` integrand
+    points per observation point summed over the timed steps."""
+    pts = npts * per_obs_total / launches        # integrand points per launch
     if precision == "mixed":
         flops = INTEGRAL_FLOPS_PER_POINT * pts
         peak = fma_peaks["fp32_tflops"]
@@ -822,7 +841,8 @@ def roofline(kname, launch_ms, launches, K, npts, wl, run, fma_peaks, hbm, preci
                                "integrand point (FMA = 2) as counted by ncu on this kernel, "
                                f"{pts:.3g} integrand points per launch",
                 "peak_source": "measured FP32 FMA rate of this GPU (peaks_measured)",
-                "binding": INTEGRAL_BINDING}
+                "binding": INTEGRAL_BINDING,
+                "issue": issue_bound(pts, launch_ms, clock_mhz, n_sms)}
     flops = 300 * pts
     peak = fma_peaks["fp64_tflops"]
     achieved = flops / (launch_ms * 1e-3) / 1e12
@@ -833,16 +853,33 @@ def roofline(kname, launch_ms, launches, K, npts, wl, run, fma_peaks, hbm, preci
 
 
 # From an ncu capture of wake_mixed_integral on this workload at a 4-region
-# step (profiles/wake_mixed_integral_chicane.md): FP32 operations per
-# integrand point (207.0 M FFMA x 2 + 938.2 M FADD/FMUL warp instructions x
-# 32 lanes / 2.048e8 points), DRAM bytes per integrand point (376.5 + 38.6
-# MB / 2.048e8), and the binding unit.
-INTEGRAL_FLOPS_PER_POINT = 211
-INTEGRAL_DRAM_BYTES_PER_POINT = 2.03
-INTEGRAL_BINDING = ("latency of the history gathers at 24 warps per SM (long-scoreboard stalls "
-                    "3.6 per issued instruction; issue 61 %, FMA pipe 47 %, L1TEX 67 %, L1 hits "
-                    "21 %, L2 hits 95 %); the FP32 mix is mostly FADD (double-word arithmetic), "
-                    "so the FMA-rate peak overstates what the pipe can reach")
+# step (profiles/wake_mixed_integral_chicane.md, 2.048e8 integrand points):
+# FP32 operations per integrand point from the executed (predicated-on)
+# thread instructions (24.03e9 FADD + 3.26e9 FMUL + 2 x 6.11e9 FFMA), DRAM
+# bytes per integrand point (343.7 + 4.3 MB), warp instructions per
+# integrand point (1468.3e6 issued), and the binding unit.
+INTEGRAL_FLOPS_PER_POINT = 193
+INTEGRAL_DRAM_BYTES_PER_POINT = 1.70
+INTEGRAL_WARP_INSTR_PER_POINT = 7.17
+INTEGRAL_BINDING = ("instruction issue (62.8 % of issue slots used at 16 warps per SM; stalls per "
+                    "issued instruction: long-scoreboard 1.3, not-selected 1.3, wait 1.0, barrier "
+                    "0.8); FMA pipe 51 %, L1TEX 56 %, L2 hits 94 %, DRAM 2 %; the FP32 mix is "
+                    "mostly FADD (double-word arithmetic: 117 FADD, 30 FFMA, 16 FMUL per "
+                    "integrand point), so the FMA-rate peak overstates what the pipe can reach")
+
+
+def issue_bound(pts, launch_ms, clock_mhz, n_sms):
+    """The integral against its instruction-issue ceiling: one warp
+    instruction per cycle on each of an SM's four schedulers, at the SM clock
+    sampled during the timed region."""
+    if not clock_mhz:
+        return None
+    need = INTEGRAL_WARP_INSTR_PER_POINT * pts
+    ideal_ms = need / (n_sms * 4 * clock_mhz * 1e6) * 1e3
+    return {"warp_instructions_per_launch": need, "ideal_ms": ideal_ms, "launch_ms": launch_ms,
+            "frac": ideal_ms / launch_ms, "clock_mhz": clock_mhz, "sms": n_sms,
+            "how": "%.2f warp instructions per integrand point (ncu) / (SMs x 4 schedulers x SM "
+                   "clock)" % INTEGRAL_WARP_INSTR_PER_POINT}
 
 
 def stage_rooflines(kt, K, wl, run, hbm, fma_peaks):

@@ -100,6 +100,24 @@ int dfcsr_deposit_cic2d(const double *q1, const double *q2, const double *w0,
                         double *out0, double *out1,
                         void *workspace, size_t workspace_bytes, void *stream);
 
+/* The same deposit on the grid of get_DF (deposit.py:147-159) taken from the
+ * beam moments in DEVICE memory (`moments`: the 16 values of
+ * dfcsr_beam_moments; [1], [2] the means of q1 and q2, [3], [4] their
+ * standard deviations): start = mean - lim sigma, end = mean + lim sigma per
+ * axis, computed by a kernel on `stream` in the host's operation order, so
+ * the result equals dfcsr_deposit_cic2d with the grid computed on the host
+ * from the same moments.  Lets a caller enqueue the deposit right behind the
+ * moments, before it has their host copy (a kick-feedback step loop waits
+ * for that copy).  A zero standard deviation (empty bin range) cannot be
+ * reported from the device: every particle then falls outside the grid; the
+ * caller checks its host copy of the moments.  Same workspace as
+ * dfcsr_deposit_cic2d. */
+int dfcsr_deposit_cic2d_moments(const double *q1, const double *q2, const double *w0,
+                                const double *w1, int64_t n, int nb1, int nb2,
+                                const double *moments, double lim1, double lim2,
+                                double *out0, double *out1,
+                                void *workspace, size_t workspace_bytes, void *stream);
+
 /* Deposit that allocates nothing.  No counterpart in the reference.  For
  * callers that cannot allocate device memory when they deposit (a host code
  * that plans its device buffers up front and forbids allocation inside its
@@ -334,7 +352,11 @@ int dfcsr_transport6(const double *R, double *coords, int64_t n, int64_t ld, voi
  * RegularGridInterpolator (linear, fill 0) at (x_transform, z) with
  * x_transform = x - (slope0 * z + slope1), pz += dE term, and px += x-kick
  * term when transverse_on.  dE_dct / x_kick: [nx, nz] row-major; xrange
- * [nx], zrange [nz] ascending.  Scratch: dfcsr_apply_wakes_workspace_bytes. */
+ * [nx], zrange [nz] strictly ascending (as the interpolator requires).
+ * Scratch (16-byte aligned): dfcsr_apply_wakes_workspace_bytes - the scaled
+ * tables and, per axis interval, its width and reciprocal (the weights are
+ * then the reference's divisions, correctly rounded, without a division per
+ * particle). */
 size_t dfcsr_apply_wakes_workspace_bytes(int nx, int nz);
 int dfcsr_apply_wakes(double *coords, int64_t n, int64_t ld, const double *dE_dct,
                       const double *x_kick, const double *xrange, const double *zrange,

@@ -19,6 +19,7 @@ with the reference); ``'mixed'`` - FP32 bulk with the retarded geometry in
 double-word FP32 (~48 bits);
 ``'both'`` keeps both history rings so either can be called.
 """
+import ctypes
 import datetime
 import os
 
@@ -82,6 +83,39 @@ def jobs_to_device(jobs, device=None):
     host = torch.frombuffer(bytearray(raw), dtype=torch.uint8)
     return host.pin_memory().to(device or torch.device("cuda", torch.cuda.current_device()),
                                 non_blocking=True)
+
+
+class _JobSlots:
+    """A ring of pinned host buffers and device buffers for single-job wakes
+    of one CSR2D: each wake fills the next slot.  A slot's host buffer is
+    rewritten once the copy out of it (four wakes earlier) has run, and its
+    device buffer is read by that earlier wake before the new copy runs when
+    both are on the same stream; a wake on another stream gets fresh
+    buffers."""
+    SLOTS = 4
+
+    def __init__(self):
+        n = ctypes.sizeof(_lib.WakeJob)
+        self.host = [torch.empty(n, dtype=torch.uint8, pin_memory=True) for _ in range(self.SLOTS)]
+        self.dev = [torch.empty(n, dtype=torch.uint8, device="cuda") for _ in range(self.SLOTS)]
+        self.event = [None] * self.SLOTS
+        self.stream = None
+        self.next = 0
+
+    def upload(self, job, stream):
+        if self.stream is not None and self.stream != stream.cuda_stream:
+            return jobs_to_device([job])
+        k = self.next
+        self.next = (k + 1) % self.SLOTS
+        if self.event[k] is not None:
+            self.event[k].synchronize()
+        ctypes.memmove(self.host[k].data_ptr(), ctypes.addressof(job), ctypes.sizeof(job))
+        with torch.cuda.stream(stream):
+            self.dev[k].copy_(self.host[k], non_blocking=True)
+            self.event[k] = torch.cuda.Event()
+            self.event[k].record(stream)
+        self.stream = stream.cuda_stream
+        return self.dev[k]
 
 
 class WakeEvaluator:
@@ -169,6 +203,7 @@ class CSR2D:
         self.parallel = False
         self.evaluator = WakeEvaluator(workspace)
         self._jobs_dev = None
+        self._job_slot = None
         self._mesh = None
         self._mesh_host = None
         self._pending = None
@@ -282,7 +317,10 @@ class CSR2D:
         keeps the results on the device checks the DF finalisations with
         ``DF_tracker.check_status()`` when it next synchronises."""
         kind = self._wake_kind(precision)
-        jobs = jobs_to_device([self._job()])
+        if self._job_slot is None:
+            self._job_slot = _JobSlots()
+        jobs = self._job_slot.upload(self._job(),
+                                     stream if stream is not None else torch.cuda.current_stream())
         self._jobs_dev = jobs
         ip = self.integration_params
         if kind == "fp64":

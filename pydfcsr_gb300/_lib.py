@@ -112,6 +112,8 @@ _SIGS = [
     ("dfcsr_deposit_workspace_bytes", _c_size, [_c_i64, _c_int, _c_int]),
     ("dfcsr_deposit_cic2d", _c_int, [_p, _p, _p, _p, _c_i64, _c_int, _c_double, _c_double,
                                       _c_int, _c_double, _c_double, _p, _p, _p, _c_size, _p]),
+    ("dfcsr_deposit_cic2d_moments", _c_int, [_p, _p, _p, _p, _c_i64, _c_int, _c_int, _p,
+                                              _c_double, _c_double, _p, _p, _p, _c_size, _p]),
     ("dfcsr_deposit_noalloc_max_bytes", _c_size, []),
     ("dfcsr_deposit_cic2d_noalloc", _c_int, [_p, _p, _p, _p, _c_i64, _c_int, _c_double, _c_double,
                                               _c_int, _c_double, _c_double, _p, _p, _p]),

@@ -146,14 +146,24 @@ class Beam:
         _lib.call("dfcsr_transport6", Rh.ctypes.data_as(ctypes.c_void_p), ptr(self.particle), n,
                   self.particle.stride(0), stream_handle())
 
-    def track(self, R, step_size, update_step=True):
+    def track(self, R, step_size, update_step=True, wait=True):
         """Apply a 6x6 transfer matrix and advance (beams.py:101-106 with a
-        linear matrix in place of bmadx's track_element)."""
+        linear matrix in place of bmadx's track_element).  ``wait=False``
+        (extension) enqueues the statistics without waiting for them (see
+        :meth:`update_status`); :attr:`moments_device` is then usable at
+        once, e.g. to enqueue the step's deposit before the host has them."""
         self.transport(R)
         self.position += step_size
         if update_step:
             self.step += 1
-        self.update_status()
+        self.update_status(wait=wait)
+
+    @property
+    def moments_device(self):
+        """(extension) The latest beam moments (dfcsr_beam_moments) as a CUDA
+        float64 tensor, including those still being copied to the host."""
+        pending = getattr(self, "_pending_status", None)
+        return pending.device if pending is not None else self._moments_dev
 
     def apply_wakes(self, dE_dct, x_kick, xrange, zrange, step_size, transverse_on, update=True):
         """Kick pz (and px when ``transverse_on``) by the wake interpolated at

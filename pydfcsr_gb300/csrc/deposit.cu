@@ -140,14 +140,22 @@ __device__ __forceinline__ bool is_nan_bits(double v) {
     return (__double_as_longlong(v) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
 }
 
+// Grid of a deposit: first bin edge and inverse spacing per axis.  Passed by
+// value, or (gp non-null) read from device memory, where a kernel of the
+// same stream wrote it from the beam's moments.
+struct DepGrid {
+    double start1, inv1, start2, inv2;
+};
+
 __global__ void cic_keys(const double *__restrict__ q1, const double *__restrict__ q2, int64_t n,
-                         int nb1, double start1, double inv1, int nb2, double start2, double inv2,
+                         int nb1, int nb2, DepGrid g, const DepGrid *__restrict__ gp,
                          uint32_t nkeys, uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (gp) g = *gp;
     const double a = q1[i], b = q2[i];
-    const int i1 = __double2int_rd(__dmul_rn(__dsub_rn(a, start1), inv1));
-    const int i2 = __double2int_rd(__dmul_rn(__dsub_rn(b, start2), inv2));
+    const int i1 = __double2int_rd(__dmul_rn(__dsub_rn(a, g.start1), g.inv1));
+    const int i2 = __double2int_rd(__dmul_rn(__dsub_rn(b, g.start2), g.inv2));
     uint32_t key = nkeys;
     if (i1 >= -1 && i1 < nb1 && i2 >= -1 && i2 < nb2 && !is_nan_bits(a) && !is_nan_bits(b))
         key = (uint32_t)(i1 + 1) * (uint32_t)(nb2 + 1) + (uint32_t)(i2 + 1);
@@ -415,8 +423,10 @@ seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, i
          uint32_t nkeys, int nb2, const uint32_t *__restrict__ cstart, const uint32_t *__restrict__ cend,
          const double *__restrict__ q1, const double *__restrict__ q2,
          const double *__restrict__ w0, const double *__restrict__ w1,
-         double start1, double inv1, double start2, double inv2,
+         DepGrid g, const DepGrid *__restrict__ gp,
          double *__restrict__ partial, double *__restrict__ chunk_first, double *__restrict__ chunk_last) {
+    if (gp) g = *gp;
+    const double inv1 = g.inv1, inv2 = g.inv2;
     __shared__ uint32_t sk[SEG_TILE + SEG_TILE / SEG_K];
     __shared__ uint32_t sv[SEG_TILE + SEG_TILE / SEG_K];
     const int64_t base = (int64_t)blockIdx.x * SEG_TILE;
@@ -435,7 +445,7 @@ seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, i
     // so the FP64 work runs on full warps; only the flush at the end of a
     // run (integer work and stores) diverges.
     uint32_t k = m > 0 ? sk[seg_slot(off)] : nkeys;
-    const double s1i = __dmul_rn(start1, inv1), s2i = __dmul_rn(start2, inv2);
+    const double s1i = __dmul_rn(g.start1, inv1), s2i = __dmul_rn(g.start2, inv2);
     double fi1 = __dadd_rn(s1i, (double)((int)(k / (uint32_t)(nb2 + 1)) - 1));
     double fi2 = __dadd_rn(s2i, (double)((int)(k % (uint32_t)(nb2 + 1)) - 1));
     double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -569,7 +579,8 @@ static DepositLayout deposit_layout(int64_t n, int nb1, int nb2) {
 
 static size_t deposit_carve(Carver &c, int64_t n, const DepositLayout &L, uint32_t **ka,
                             uint32_t **va, uint32_t **kb, uint32_t **vb, uint32_t **hist,
-                            uint32_t **dtot, uint32_t **cs, uint32_t **ce, double **part) {
+                            uint32_t **dtot, uint32_t **cs, uint32_t **ce, double **part,
+                            DepGrid **grid) {
     const size_t nn = (size_t)(n > 0 ? n : 1);
     // the four sort buffers hold a multiple of SEG_K entries: after the sort
     // the idle pair (4 B x that many each) is reused as the seg_sums chunk
@@ -584,6 +595,7 @@ static size_t deposit_carve(Carver &c, int64_t n, const DepositLayout &L, uint32
     *cs = c.take<uint32_t>((size_t)L.nkeys + 1);
     *ce = c.take<uint32_t>((size_t)L.nkeys + 1);
     *part = c.take<double>((size_t)L.nkeys * 8);
+    *grid = c.take<DepGrid>(1);
     return c.used;
 }
 
@@ -629,44 +641,72 @@ extern "C" size_t dfcsr_deposit_workspace_bytes(int64_t n, int nb1, int nb2) {
     Carver c{nullptr, 0, 0};
     uint32_t *a, *b, *cc, *d, *e, *f, *g, *h;
     double *p;
-    return deposit_carve(c, n, L, &a, &b, &cc, &d, &e, &f, &g, &h, &p) + 256;
+    DepGrid *gr;
+    return deposit_carve(c, n, L, &a, &b, &cc, &d, &e, &f, &g, &h, &p, &gr) + 256;
 }
 
-extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const double *w0,
-                                   const double *w1, int64_t n, int nb1, double start1,
-                                   double end1, int nb2, double start2, double end2,
-                                   double *out0, double *out1, void *workspace,
-                                   size_t workspace_bytes, void *stream) {
-    clear_error();
-    DFCSR_CHECK_ARG(out0, "dfcsr_deposit_cic2d: out0 is null");
-    DFCSR_CHECK_ARG(nb1 > 0 && nb2 > 0, "dfcsr_deposit_cic2d: bins must be positive (%d, %d)", nb1, nb2);
-    DFCSR_CHECK_ARG(((int64_t)nb1 + 1) * ((int64_t)nb2 + 1) < (1ll << 30),
-                    "dfcsr_deposit_cic2d: grid %d x %d too large", nb1, nb2);
-    DFCSR_CHECK_ARG(n >= 0 && n < (1ll << 32) - 1, "dfcsr_deposit_cic2d: bad particle count %lld",
-                    (long long)n);
-    DFCSR_CHECK_ARG(n == 0 || (q1 && q2), "dfcsr_deposit_cic2d: null coordinates");
-    DFCSR_CHECK_ARG(end1 != start1 && end2 != start2, "dfcsr_deposit_cic2d: empty bin range");
-    DFCSR_CHECK_ARG(!(out1 && n > 0 && !w1), "dfcsr_deposit_cic2d: out1 given without w1");
-    cudaStream_t s = as_stream(stream);
+// The grid of get_DF (deposit.py:147-159) from the beam moments on the
+// device (m[1], m[2]: means of x and z; m[3], m[4]: their standard
+// deviations): start = mean - lim sigma, end = mean + lim sigma, and the
+// deposit's inverse spacing 1 / ((end - start) / nbins), in the host's
+// operation order.  One thread.
+__global__ void grid_from_moments(const double *__restrict__ m, double lim1, double lim2, int nb1,
+                                  int nb2, DepGrid *__restrict__ out) {
+    const double s1 = __dsub_rn(m[1], __dmul_rn(lim1, m[3]));
+    const double e1 = __dadd_rn(m[1], __dmul_rn(lim1, m[3]));
+    const double s2 = __dsub_rn(m[2], __dmul_rn(lim2, m[4]));
+    const double e2 = __dadd_rn(m[2], __dmul_rn(lim2, m[4]));
+    out->start1 = s1;
+    out->inv1 = __ddiv_rn(1.0, __ddiv_rn(__dsub_rn(e1, s1), (double)nb1));
+    out->start2 = s2;
+    out->inv2 = __ddiv_rn(1.0, __ddiv_rn(__dsub_rn(e2, s2), (double)nb2));
+}
+
+static int deposit_check(const char *fn, const double *q1, const double *q2, const double *w1,
+                         int64_t n, int nb1, int nb2, double *out0, double *out1) {
+    DFCSR_CHECK_ARG(out0, "%s: out0 is null", fn);
+    DFCSR_CHECK_ARG(nb1 > 0 && nb2 > 0, "%s: bins must be positive (%d, %d)", fn, nb1, nb2);
+    DFCSR_CHECK_ARG(((int64_t)nb1 + 1) * ((int64_t)nb2 + 1) < (1ll << 30), "%s: grid %d x %d too large",
+                    fn, nb1, nb2);
+    DFCSR_CHECK_ARG(n >= 0 && n < (1ll << 32) - 1, "%s: bad particle count %lld", fn, (long long)n);
+    DFCSR_CHECK_ARG(n == 0 || (q1 && q2), "%s: null coordinates", fn);
+    DFCSR_CHECK_ARG(!(out1 && n > 0 && !w1), "%s: out1 given without w1", fn);
+    return DFCSR_OK;
+}
+
+// Keys, sort, per-cell sums and assembly on stream s.  The grid is `g`, or
+// the DepGrid that grid_from_moments writes into the workspace first when
+// `moments` is given.
+static int deposit_run(const char *fn, const double *q1, const double *q2, const double *w0,
+                       const double *w1, int64_t n, int nb1, int nb2, DepGrid g,
+                       const double *moments, double lim1, double lim2, double *out0, double *out1,
+                       void *workspace, size_t workspace_bytes, cudaStream_t s) {
     const DepositLayout L = deposit_layout(n, nb1, nb2);
     Carver c{reinterpret_cast<char *>(workspace), workspace_bytes, 0};
     uint32_t *ka, *va, *kb, *vb, *hist, *dtot, *cs, *ce;
     double *part;
-    deposit_carve(c, n, L, &ka, &va, &kb, &vb, &hist, &dtot, &cs, &ce, &part);
+    DepGrid *gslot;
+    deposit_carve(c, n, L, &ka, &va, &kb, &vb, &hist, &dtot, &cs, &ce, &part, &gslot);
     if (!workspace || !c.ok()) {
-        set_error("dfcsr_deposit_cic2d: workspace too small (%zu < %zu)", workspace_bytes, c.used);
+        set_error("%s: workspace too small (%zu < %zu)", fn, workspace_bytes, c.used);
         return DFCSR_OOM;
     }
-    const double inv1 = 1.0 / ((end1 - start1) / nb1);
-    const double inv2 = 1.0 / ((end2 - start2) / nb2);
+    const DepGrid *gp = nullptr;
+    if (moments) {
+        note_launch();
+        grid_from_moments<<<1, 1, 0, s>>>(moments, lim1, lim2, nb1, nb2, gslot);
+        gp = gslot;
+    }
     DFCSR_CUDA_TRY(cudaMemsetAsync(cs, 0, sizeof(uint32_t) * ((size_t)L.nkeys + 1), s));
     DFCSR_CUDA_TRY(cudaMemsetAsync(ce, 0, sizeof(uint32_t) * ((size_t)L.nkeys + 1), s));
+    // timed from here: on a second stream the memsets above can wait for SM
+    // space behind another stream's persistent kernel
     ScopedTiming tm("deposit_cic2d", s);
     if (n > 0) {
         const int tb = 256;
         note_launch();
-        cic_keys<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(q1, q2, n, nb1, start1, inv1, nb2,
-                                                              start2, inv2, L.nkeys, ka, va);
+        cic_keys<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(q1, q2, n, nb1, nb2, g, gp, L.nkeys, ka,
+                                                              va);
         uint32_t *kin = ka, *vin = va, *kout = kb, *vout = vb;
         for (int p = 0; p < L.passes; ++p) {
             const int shift = RS_BITS * p;
@@ -687,7 +727,7 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
         const unsigned sb = (unsigned)((n + SEG_TILE - 1) / SEG_TILE);
 #define DFCSR_SEG(A, B)                                                                       \
     seg_sums<A, B><<<sb, SEG_THREADS, 0, s>>>(kin, vin, n, L.nkeys, nb2, cs, ce, q1, q2, w0, w1, \
-                                              start1, inv1, start2, inv2, part, cfirst, clast)
+                                              g, gp, part, cfirst, clast)
         note_launch();
         if (w0 && w1) DFCSR_SEG(true, true);
         else if (w0) DFCSR_SEG(true, false);
@@ -705,4 +745,36 @@ extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const dou
     cic_assemble<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(part, nb1, nb2, out0, out1);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
+}
+
+extern "C" int dfcsr_deposit_cic2d(const double *q1, const double *q2, const double *w0,
+                                   const double *w1, int64_t n, int nb1, double start1,
+                                   double end1, int nb2, double start2, double end2,
+                                   double *out0, double *out1, void *workspace,
+                                   size_t workspace_bytes, void *stream) {
+    clear_error();
+    const int st = deposit_check("dfcsr_deposit_cic2d", q1, q2, w1, n, nb1, nb2, out0, out1);
+    if (st != DFCSR_OK) return st;
+    DFCSR_CHECK_ARG(end1 != start1 && end2 != start2, "dfcsr_deposit_cic2d: empty bin range");
+    DepGrid g;
+    g.start1 = start1;
+    g.inv1 = 1.0 / ((end1 - start1) / nb1);
+    g.start2 = start2;
+    g.inv2 = 1.0 / ((end2 - start2) / nb2);
+    return deposit_run("dfcsr_deposit_cic2d", q1, q2, w0, w1, n, nb1, nb2, g, nullptr, 0.0, 0.0,
+                       out0, out1, workspace, workspace_bytes, as_stream(stream));
+}
+
+extern "C" int dfcsr_deposit_cic2d_moments(const double *q1, const double *q2, const double *w0,
+                                           const double *w1, int64_t n, int nb1, int nb2,
+                                           const double *moments, double lim1, double lim2,
+                                           double *out0, double *out1, void *workspace,
+                                           size_t workspace_bytes, void *stream) {
+    clear_error();
+    const int st = deposit_check("dfcsr_deposit_cic2d_moments", q1, q2, w1, n, nb1, nb2, out0, out1);
+    if (st != DFCSR_OK) return st;
+    DFCSR_CHECK_ARG(moments, "dfcsr_deposit_cic2d_moments: moments is null");
+    DFCSR_CHECK_ARG(lim1 > 0.0 && lim2 > 0.0, "dfcsr_deposit_cic2d_moments: limits must be positive");
+    return deposit_run("dfcsr_deposit_cic2d_moments", q1, q2, w0, w1, n, nb1, nb2, DepGrid{}, moments,
+                       lim1, lim2, out0, out1, workspace, workspace_bytes, as_stream(stream));
 }

@@ -38,7 +38,10 @@
 
 namespace dfcsr {
 
-constexpr int MX_THREADS = 256;
+#ifndef MX_INTEGRAL_THREADS
+#define MX_INTEGRAL_THREADS 256
+#endif
+constexpr int MX_THREADS = MX_INTEGRAL_THREADS;
 constexpr int MX_CHUNK = 128;       // s' columns staged in shared memory at once
 constexpr int MX_MAX_ROWS = 1024;   // x' rows per region (2 * xbins)
 constexpr int MX_MAX_COLS = 4096;   // s' columns per region (zbins)
@@ -1032,10 +1035,28 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
 
 // Persistent: CTAs take points of the batch from a work counter.  Writes the
 // FP64 region sums part[b][r][2].
+//
+// Launch shape: 256-thread CTAs capped at MX_INTEGRAL_MAXREG (120) registers
+// per thread.  The kernel needs ~125 registers without spills and has none
+// at 120; two CTAs then fit on an SM and leave 4096 of its 65,536 registers
+// to one 128-thread, 32-register CTA of the beam-moments kernel, which runs
+// on a second stream beside the wake in a pipelined step loop.  Three CTAs
+// per SM (80 registers) spill ~240 bytes per thread (a third of the kernel's
+// L2 traffic) and measured 8 % slower; 128 registers leave no room for the
+// moments CTA, which then waits for the whole integral.  Defining
+// MX_INTEGRAL_MAXREG as 0 selects __launch_bounds__ with
+// MX_INTEGRAL_BLOCKS CTAs per SM instead.
+#ifndef MX_INTEGRAL_MAXREG
+#define MX_INTEGRAL_MAXREG 120
+#endif
 #ifndef MX_INTEGRAL_BLOCKS
 #define MX_INTEGRAL_BLOCKS 3
 #endif
+#if MX_INTEGRAL_MAXREG > 0
+__global__ void __maxnreg__(MX_INTEGRAL_MAXREG)
+#else
 __global__ void __launch_bounds__(MX_THREADS, MX_INTEGRAL_BLOCKS)
+#endif
 mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
                int64_t first, int64_t count, size_t rec_words, const float *__restrict__ rec,
                const PointMeta *__restrict__ meta, const int2 *__restrict__ rows_valid,

@@ -74,6 +74,29 @@ def deposit_cic(q1, q2, w0, w1, nbins_1, bins_start_1, bins_end_1, nbins_2, bins
     return out0, out1
 
 
+def deposit_cic_from_moments(q1, q2, w0, w1, nbins_1, nbins_2, moments, lim_1, lim_2, stream=None,
+                             ws=None, out0=None, out1=None):
+    """(extension) :func:`deposit_cic` on the grid mean -+ lim sigma per axis
+    taken from ``moments`` (a CUDA float64 tensor of dfcsr_beam_moments) on
+    the device: nothing waits for the host."""
+    require_cuda()
+    n = q1.numel()
+    ws = ws or default_workspace()
+    nb1, nb2 = int(nbins_1), int(nbins_2)
+    if moments.dtype != torch.float64 or not moments.is_cuda or moments.numel() < 5:
+        raise ValueError("moments must be a CUDA float64 tensor of dfcsr_beam_moments")
+    if out0 is None:
+        out0 = torch.empty((nb1, nb2), dtype=torch.float64, device=q1.device)
+    if out1 is None and w1 is not None:
+        out1 = torch.empty((nb1, nb2), dtype=torch.float64, device=q1.device)
+    need = _lib.query("dfcsr_deposit_workspace_bytes", n, nb1, nb2)
+    buf = ws.get("deposit", need)
+    _lib.call("dfcsr_deposit_cic2d_moments", ptr(q1), ptr(q2), ptr(w0), ptr(w1), n, nb1, nb2,
+              ptr(moments.contiguous()), float(lim_1), float(lim_2), ptr(out0), ptr(out1),
+              ptr(buf), buf.numel(), stream_handle(stream))
+    return out0, out1
+
+
 def histogram_cic_2d(q1, q2, w, nbins_1, bins_start_1, bins_end_1, nbins_2, bins_start_2,
                      bins_end_2):
     """2D cloud-in-cell histogram of ``q1``, ``q2`` weighted by ``w``.
@@ -177,8 +200,9 @@ class HistoryRing:
 
 class PendingDeposit:
     """A deposit enqueued by :meth:`DF_tracker.deposit_DF`: the host moments
-    it was sized from, the field array [5, nx, nz] (channels 0 and 3 written
-    by the deposit) and the event recorded after it."""
+    it was sized from (None when the grid came from the device moments), the
+    field array [5, nx, nz] (channels 0 and 3 written by the deposit) and the
+    event recorded after it."""
     __slots__ = ("moments", "fields", "event")
 
     def __init__(self, moments, fields, event):
@@ -292,18 +316,39 @@ class DF_tracker:
         return xb, zb, win, x0, x1, z0, z1
 
     def deposit_DF(self, x, z, px, moments, stream=None):
-        """(extension) The deposit half of get_DF, for particles whose host
-        moments are already known: the grid from ``moments``, both CIC
-        channels into a new field array, enqueued on ``stream`` (default:
-        the current stream).  Returns a :class:`PendingDeposit` to hand to
-        ``get_DF(..., deposited=...)``; the tracker's state is not touched,
-        so the deposit of a later step can run while this step is finalised.
-        ``x``, ``z``, ``px`` must stay unchanged until the deposit has run.
-        Deposits of one tracker share its deposit scratch: two of them must
-        not be in flight on different streams at once."""
+        """(extension) The deposit half of get_DF: the grid from ``moments``,
+        both CIC channels into a new field array, enqueued on ``stream``
+        (default: the current stream).  Returns a :class:`PendingDeposit` to
+        hand to ``get_DF(..., deposited=...)``; the tracker's state is not
+        touched, so the deposit of a later step can run while this step is
+        finalised.  ``x``, ``z``, ``px`` must stay unchanged until the
+        deposit has run.  Deposits of one tracker share its deposit scratch:
+        two of them must not be in flight on different streams at once.
+
+        ``moments`` is the host array of dfcsr_beam_moments, or the CUDA
+        tensor itself (e.g. ``beam.moments_device`` while its copy to the
+        host is in flight): with the configured grid rule the deposit then
+        takes its grid from the device moments and nothing waits for the
+        host; get_DF receives the host copy later through its ``moments``
+        argument (``CSR2D.update_history`` passes the beam's)."""
         require_cuda()
-        st = np.asarray(moments, dtype=np.float64)
         s = stream if stream is not None else torch.cuda.current_stream()
+        if isinstance(moments, torch.Tensor):
+            if self.grid_rule == "configured":
+                # the grid from the device moments, by the deposit's first kernel
+                xb, zb = int(self.xbins), int(self.zbins)
+                with torch.cuda.stream(s):
+                    xd, zd, pxd = (as_device_f64(a).reshape(-1) for a in (x, z, px))
+                    fields = torch.empty((5, xb, zb), dtype=torch.float64, device=xd.device)
+                    deposit_cic_from_moments(xd, zd, None, pxd, xb, zb, moments, self.xlim,
+                                             self.zlim, s, self._workspace(), out0=fields[0],
+                                             out1=fields[3])
+                    ev = torch.cuda.Event()
+                    ev.record(s)
+                return PendingDeposit(None, fields, ev)
+            # the reference's rule picks the bins from the moments: host copy
+            moments = moments.cpu().numpy()
+        st = np.asarray(moments, dtype=np.float64)
         xb, zb, win, x0, x1, z0, z1 = self._grid(st)
         with torch.cuda.stream(s):
             xd, zd, pxd = (as_device_f64(a).reshape(-1) for a in (x, z, px))
@@ -334,6 +379,14 @@ class DF_tracker:
         fields = deposited.fields
         fields.record_stream(s)
         st = deposited.moments
+        if st is None:      # sized on the device from the moments: their host copy
+            if moments is None:
+                raise ValueError("get_DF: a deposit sized from device moments needs the host "
+                                 "moments (the 'moments' argument)")
+            st = np.asarray(moments, dtype=np.float64)
+            _, _, _, x0, x1, z0, z1 = self._grid(st)
+            if x1 == x0 or z1 == z0:
+                raise ValueError("dfcsr_deposit_cic2d_moments: empty bin range")
         self.stats = st
         sigma_x, sigma_z = float(st[3]), float(st[4])
         self.sigma_x, self.sigma_z = sigma_x, sigma_z

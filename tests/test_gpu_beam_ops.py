@@ -51,6 +51,36 @@ def test_apply_wakes_capi_matches_reference():
         np.testing.assert_array_equal(out, ref)
 
 
+@pytest.mark.parametrize("slope", [(0.0, 0.0), (-0.37, 2.5e-6)])
+def test_apply_wakes_capi_bitexact_large(slope):
+    """600,000 particles against the oracle bit for bit: random positions
+    over and beyond a 64 x 80 mesh, particles exactly on grid lines and on
+    the end points (with slope 0, x_transform = x exactly), and x = -0.  The
+    kernel's weights come from per-interval reciprocals and one FMA
+    correction, which must reproduce the reference's divisions exactly."""
+    rng = np.random.default_rng(11)
+    nx, nz, n = 64, 80, 600_000
+    xr = np.linspace(-3.1e-5, 2.9e-5, nx)
+    zr = np.linspace(-1.6e-4, 1.4e-4, nz)
+    c = np.zeros((6, n))
+    c[0] = rng.uniform(-3.6e-5, 3.4e-5, n)
+    c[4] = rng.uniform(-1.8e-4, 1.6e-4, n)
+    c[1] = rng.normal(0, 1e-6, n)
+    c[5] = rng.normal(0, 1e-4, n)
+    k = n // 8
+    c[0, :k] = xr[rng.integers(0, nx, k)]
+    c[4, k:2 * k] = zr[rng.integers(0, nz, k)]
+    c[0, 2 * k:2 * k + 4], c[4, 2 * k:2 * k + 4] = [xr[0], xr[-1], xr[0], xr[-1]], [zr[0], zr[-1], zr[-1], zr[0]]
+    c[0, 2 * k + 4] = -0.0
+    g = {"dE_dct": rng.normal(0, 3e3, (nx, nz)), "x_kick": rng.normal(0, 1e2, (nx, nz)),
+         "xrange": xr, "zrange": zr, "step_size": 0.013, "init_energy": 1e9}
+    for transverse in (True, False):
+        out = _call_apply(c, g, transverse, slope)
+        ref = O.apply_wakes(c, g["dE_dct"], g["x_kick"], xr, zr, g["step_size"], g["init_energy"],
+                            transverse, np.array(slope))
+        np.testing.assert_array_equal(out, ref)
+
+
 def test_beam_apply_wakes_vs_oracle():
     from pydfcsr_gb300.beams import Beam
     g = golden("apply_wakes.npz")
