@@ -39,10 +39,13 @@
 namespace dfcsr {
 
 #ifndef MX_INTEGRAL_THREADS
-#define MX_INTEGRAL_THREADS 256
+#define MX_INTEGRAL_THREADS 128
 #endif
 constexpr int MX_THREADS = MX_INTEGRAL_THREADS;
-constexpr int MX_CHUNK = 128;       // s' columns staged in shared memory at once
+#ifndef MX_INTEGRAL_CHUNK
+#define MX_INTEGRAL_CHUNK 128
+#endif
+constexpr int MX_CHUNK = MX_INTEGRAL_CHUNK;   // s' columns staged in shared memory at once
 constexpr int MX_MAX_ROWS = 1024;   // x' rows per region (2 * xbins)
 constexpr int MX_MAX_COLS = 4096;   // s' columns per region (zbins)
 constexpr int GEO_THREADS = 128;
@@ -870,7 +873,7 @@ __device__ __forceinline__ void kahan(float &s, float &c, float v) {
 struct IntegralSmem {
     float4 col[MX_CHUNK * CW / 4];
     float4 red[MX_THREADS / 32];
-    long long pt;
+    long long pt[2];   // the current work unit and the next one (fetched during the current)
 };
 constexpr size_t kIntegralRowOff = (sizeof(IntegralSmem) + 15) & ~(size_t)15;
 
@@ -1007,14 +1010,15 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
             A = dw_add_f(A, __fmul_rn(dsc, A.hi));
             const dw w = two_prod(wx, ws);
             const dw wr = dw_mul(w, dw_recip_from(rd, inv_r));     // w / |r - r'|
-            acc.zx = dw_add_abs(acc.zx, dw_mul(dw_mul(A, F.dx), wr));
-            // density term -scale (a + vx b) den vx_x w / |r - r'| in double-word
+            // density term -scale (a + vx b) den vx_x in double-word
             const float4 q6 = cr[6];
             const float scale = 1.f + dsc;
             const dw p1w = dw_add_f(dw{q4.x, q7.z}, __fmul_rn(vr, q4.y));
             dw Dn = dw_neg(dw_mul(two_prod(F.den, F.vxx), p1w));
             Dn = dw_add_f(Dn, __fmul_rn(dsc, Dn.hi));
-            acc.zx = dw_add_abs(acc.zx, dw_mul(Dn, wr));
+            // both double-word terms, then one product with w / |r - r'| and
+            // one accumulation (the sum's error is ~2^-48 of its terms)
+            acc.zx = dw_add_abs(acc.zx, dw_mul(dw_add_abs(dw_mul(A, F.dx), Dn), wr));
             // density_z term (FP32)
             const float wf = wx * ws;
             const float brz = q5.z - vr * fmaf(vr, q6.x, q5.w);
@@ -1036,13 +1040,17 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
 // Persistent: CTAs take points of the batch from a work counter.  Writes the
 // FP64 region sums part[b][r][2].
 //
-// Launch shape: 256-thread CTAs capped at MX_INTEGRAL_MAXREG (120) registers
+// Launch shape: 128-thread CTAs capped at MX_INTEGRAL_MAXREG (120) registers
 // per thread.  The kernel needs ~125 registers without spills and has none
-// at 120; two CTAs then fit on an SM and leave 4096 of its 65,536 registers
-// to one 128-thread, 32-register CTA of the beam-moments kernel, which runs
-// on a second stream beside the wake in a pipelined step loop.  Three CTAs
-// per SM (80 registers) spill ~240 bytes per thread (a third of the kernel's
-// L2 traffic) and measured 8 % slower; 128 registers leave no room for the
+// at 120; four CTAs then fit on an SM (16 warps) and leave 4096 of its 65,536
+// registers to one 128-thread, 32-register CTA of the beam-moments kernel,
+// which runs on a second stream beside the wake in a pipelined step loop.
+// Measured per 4-region step of the chicane benchmark (integral, ms): three
+// 256-thread CTAs at 80 registers (~240 bytes of spills per thread, a third
+// of the kernel's L2 traffic) 2.09; two 256-thread CTAs at 120 registers
+// 1.92; four 128-thread CTAs 1.76 (fewer warps wait at each unit-end
+// barrier and four work units per SM stage their records independently);
+// 96- or 64-thread CTAs 1.87 / 1.93.  128 registers leave no room for the
 // moments CTA, which then waits for the whole integral.  Defining
 // MX_INTEGRAL_MAXREG as 0 selects __launch_bounds__ with
 // MX_INTEGRAL_BLOCKS CTAs per SM instead.
@@ -1067,12 +1075,18 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
     const int tid = threadIdx.x;
     // work unit = one integration region of one point (unit u: point
     // u / WAKE_MAX_REGIONS, region u % WAKE_MAX_REGIONS), so that the CTAs
-    // finish a batch together (a region is a quarter to a half of a point)
-    for (;;) {
-        if (tid == 0) sm.pt = (long long)atomicAdd(counter, 1ull);
-        __syncthreads();
-        const int64_t u = sm.pt;
+    // finish a batch together (a region is a quarter to a half of a point).
+    // The next unit's index is taken while the current one runs, so the
+    // atomic's latency is off the CTA's critical path: slot par holds the
+    // current unit, slot par ^ 1 receives the next before the unit-end
+    // barrier, and every thread has read slot par before thread 0 reuses it
+    // one unit later.
+    if (tid == 0) sm.pt[0] = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    for (int par = 0;; par ^= 1) {
+        const int64_t u = sm.pt[par];
         if (u >= count * WAKE_MAX_REGIONS) break;
+        if (tid == 0) sm.pt[par ^ 1] = (long long)atomicAdd(counter, 1ull);
         const int64_t b = u / WAKE_MAX_REGIONS;
         const int r = (int)(u - b * WAKE_MAX_REGIONS);
         // PointMeta is read field by field: a local copy indexed by r would
