@@ -838,8 +838,10 @@ def roofline(kname, launch_ms, launches, per_obs_total, npts, fma_peaks, hbm, pr
                 "kernel": kname, "launch_ms": launch_ms, "launches": launches,
                 "integrand_points_per_launch": pts,
                 "algorithmic": f"{INTEGRAL_FLOPS_PER_POINT} FP32 floating-point operations per "
-                               "integrand point (FMA = 2) as counted by ncu on this kernel, "
-                               f"{pts:.3g} integrand points per launch",
+                               "integrand point (FMA = 2; executed thread instructions counted "
+                               f"by ncu on this kernel), {pts:.3g} integrand points per launch "
+                               "(per timed step: 40,000 per observation point in the 3-region "
+                               "branch, 50,000 in the 4-region one)",
                 "peak_source": "measured FP32 FMA rate of this GPU (peaks_measured)",
                 "binding": INTEGRAL_BINDING,
                 "issue": issue_bound(pts, launch_ms, clock_mhz, n_sms)}
@@ -855,16 +857,16 @@ def roofline(kname, launch_ms, launches, per_obs_total, npts, fma_peaks, hbm, pr
 # From an ncu capture of wake_mixed_integral on this workload at a 4-region
 # step (profiles/wake_mixed_integral_chicane.md, 2.048e8 integrand points):
 # FP32 operations per integrand point from the executed (predicated-on)
-# thread instructions (24.03e9 FADD + 3.26e9 FMUL + 2 x 6.11e9 FFMA), DRAM
-# bytes per integrand point (343.7 + 4.3 MB), warp instructions per
-# integrand point (1468.3e6 issued), and the binding unit.
-INTEGRAL_FLOPS_PER_POINT = 193
-INTEGRAL_DRAM_BYTES_PER_POINT = 1.70
-INTEGRAL_WARP_INSTR_PER_POINT = 7.17
-INTEGRAL_BINDING = ("instruction issue (62.8 % of issue slots used at 16 warps per SM; stalls per "
-                    "issued instruction: long-scoreboard 1.3, not-selected 1.3, wait 1.0, barrier "
-                    "0.8); FMA pipe 51 %, L1TEX 56 %, L2 hits 94 %, DRAM 2 %; the FP32 mix is "
-                    "mostly FADD (double-word arithmetic: 117 FADD, 30 FFMA, 16 FMUL per "
+# thread instructions (23.28e9 FADD + 3.11e9 FMUL + 2 x 5.89e9 FFMA), DRAM
+# bytes per integrand point (345.8 + 4.3 MB), warp instructions per
+# integrand point (1407.6e6 issued), and the binding unit.
+INTEGRAL_FLOPS_PER_POINT = 186
+INTEGRAL_DRAM_BYTES_PER_POINT = 1.71
+INTEGRAL_WARP_INSTR_PER_POINT = 6.87
+INTEGRAL_BINDING = ("instruction issue (68.5 % of issue slots used at 16 warps per SM; stalls per "
+                    "issued instruction: long-scoreboard 1.3, not-selected 1.2, wait 1.0, barrier "
+                    "0.3); FMA pipe 56 %, L1TEX 63 %, L2 hits 94 %, DRAM 3 %; the FP32 mix is "
+                    "mostly FADD (double-word arithmetic: 114 FADD, 29 FFMA, 15 FMUL per "
                     "integrand point), so the FMA-rate peak overstates what the pipe can reach")
 
 
