@@ -48,7 +48,10 @@ constexpr int MX_THREADS = MX_INTEGRAL_THREADS;
 constexpr int MX_CHUNK = MX_INTEGRAL_CHUNK;   // s' columns staged in shared memory at once
 constexpr int MX_MAX_ROWS = 1024;   // x' rows per region (2 * xbins)
 constexpr int MX_MAX_COLS = 4096;   // s' columns per region (zbins)
-constexpr int GEO_THREADS = 128;
+#ifndef MX_GEO_THREADS
+#define MX_GEO_THREADS 128
+#endif
+constexpr int GEO_THREADS = MX_GEO_THREADS;
 constexpr int SETUP_THREADS = 64;
 constexpr int GEO_MAXB = 6;
 
@@ -648,7 +651,10 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
 // One 128-thread CTA per observation point (six per SM): the point's set-up
 // record from mixed_setup, then the s' columns of all regions as one flat
 // range across the block, then the x' rows likewise.
-__global__ void __launch_bounds__(GEO_THREADS, 6)
+#ifndef MX_GEO_BLOCKS
+#define MX_GEO_BLOCKS 6
+#endif
+__global__ void __launch_bounds__(GEO_THREADS, MX_GEO_BLOCKS)
 mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
                const double *__restrict__ S, const double *__restrict__ X, int64_t first, int64_t count,
                const GeoShared *__restrict__ setup, size_t rec_words, float *__restrict__ rec,
@@ -936,7 +942,10 @@ struct ChunkSums {
 // z = z0 + delta / dz (a z shift reaches ~100 cells near the source, so an
 // FP32 product would misplace the gather by ~1e-5 cell); then the density_x
 // product chain w scale brx dx / |r - r'|.  The other terms are FP32.
-constexpr int MX_ROWBLK = 4;
+#ifndef MX_INTEGRAL_ROWBLK
+#define MX_INTEGRAL_ROWBLK 4
+#endif
+constexpr int MX_ROWBLK = MX_INTEGRAL_ROWBLK;
 
 template <bool DXDW>
 __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float4 *__restrict__ rows,
@@ -1003,22 +1012,22 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
                                       2u * (uint32_t)(z1 - z0), td, td_lo, xd, rw.w, zd, zd_lo);
             const float vr = F.vx.hi;
             const float4 q4 = cr[4], q5 = cr[5];
-            // density_x term: w scale brx dx / |r - r'| in double-word, with
-            // brx = K0x - vx (K1x + vx K2x) and scale = 1 + x' rho
+            // longitudinal double-word part: w scale (brx dx - (a + vx b) den
+            // vx_x) / |r - r'|, with brx = K0x - vx (K1x + vx K2x) and
+            // scale = 1 + x' rho applied once to the sum of the two terms
             const float dsc = __fmul_rn(rw.z, rho);
-            dw A = dw_sub_abs(K0x, dw_mul_f(F.vx, fmaf(vr, q5.y, q5.x + 1.f)));
-            A = dw_add_f(A, __fmul_rn(dsc, A.hi));
+            const dw A = dw_sub_abs(K0x, dw_mul_f(F.vx, fmaf(vr, q5.y, q5.x + 1.f)));
             const dw w = two_prod(wx, ws);
             const dw wr = dw_mul(w, dw_recip_from(rd, inv_r));     // w / |r - r'|
-            // density term -scale (a + vx b) den vx_x in double-word
             const float4 q6 = cr[6];
             const float scale = 1.f + dsc;
             const dw p1w = dw_add_f(dw{q4.x, q7.z}, __fmul_rn(vr, q4.y));
-            dw Dn = dw_neg(dw_mul(two_prod(F.den, F.vxx), p1w));
-            Dn = dw_add_f(Dn, __fmul_rn(dsc, Dn.hi));
-            // both double-word terms, then one product with w / |r - r'| and
-            // one accumulation (the sum's error is ~2^-48 of its terms)
-            acc.zx = dw_add_abs(acc.zx, dw_mul(dw_add_abs(dw_mul(A, F.dx), Dn), wr));
+            const dw Dn = dw_neg(dw_mul(two_prod(F.den, F.vxx), p1w));
+            // the two terms, the scale, one product with w / |r - r'| and one
+            // accumulation (the sum's error is ~2^-48 of its terms)
+            dw T = dw_add_abs(dw_mul(A, F.dx), Dn);
+            T = dw_add_f(T, __fmul_rn(dsc, T.hi));
+            acc.zx = dw_add_abs(acc.zx, dw_mul(T, wr));
             // density_z term (FP32)
             const float wf = wx * ws;
             const float brz = q5.z - vr * fmaf(vr, q6.x, q5.w);
