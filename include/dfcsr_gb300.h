@@ -180,6 +180,18 @@ typedef struct {
  * One cooperative launch (one CTA per SM, all resident) on `stream`.
  * Scratch: dfcsr_df_workspace_bytes(nx, nz). */
 size_t dfcsr_df_workspace_bytes(int nx, int nz);
+
+/* The per-step grid tables of dfcsr_df_params from get_DF's two grids,
+ * x_grids = linspace(x0, x1, nx), z_grids = linspace(z0, z1, nz)
+ * (deposit.py:170-171), on the device: gx [4][nx], gz [4][nz] (the
+ * numpy.gradient coefficients, deposit.py:212-213, edge_order 1) and dxg
+ * [nx-1], dzg [nz-1] (diff of each grid), equal to the host's numpy values
+ * bit for bit.  x_uniform / z_uniform: whether numpy takes its
+ * uniform-spacing branch (all differences equal; the caller decides it
+ * from its host grid).  One launch on `stream`, device pointers out. */
+int dfcsr_df_axis_tables(double x0, double x1, int nx, double z0, double z1, int nz,
+                         int x_uniform, int z_uniform, double *gx, double *gz,
+                         double *dxg, double *dzg, void *stream);
 int dfcsr_df_finalize(const dfcsr_df_params *p, double *density, double *vx,
                       double *density_x, double *density_z, double *vx_x,
                       double *scalars_out, void *workspace, size_t workspace_bytes,
@@ -334,6 +346,17 @@ int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
                      int xbins_max, int zbins_max, int use_band,
                      double *dE, double *xkick,
                      void *workspace, size_t workspace_bytes, void *stream);
+
+/* The same wake for one job in HOST memory (a caller's dfcsr_wake_job
+ * struct, read during the call and passed to the device as a kernel
+ * parameter): no device copy of the job to stage, no copy on the stream.
+ * Same results, workspace and limits as dfcsr_wake_mixed with that job for
+ * every point.  No reference counterpart as a separate call: it is
+ * calculate_2D_CSR (CSR.py:397-418) for one beam. */
+int dfcsr_wake_mixed_job(const dfcsr_wake_job *job, const double *s, const double *x,
+                         int64_t n, int xbins_max, int zbins_max, int use_band,
+                         double *dE, double *xkick, void *workspace,
+                         size_t workspace_bytes, void *stream);
 
 /* ------------------------------------------------------------------------
  * Particle steps on either side of the wake.  `coords` is the beam's

@@ -85,39 +85,6 @@ def jobs_to_device(jobs, device=None):
                                 non_blocking=True)
 
 
-class _JobSlots:
-    """A ring of pinned host buffers and device buffers for single-job wakes
-    of one CSR2D: each wake fills the next slot.  A slot's host buffer is
-    rewritten once the copy out of it (four wakes earlier) has run, and its
-    device buffer is read by that earlier wake before the new copy runs when
-    both are on the same stream; a wake on another stream gets fresh
-    buffers."""
-    SLOTS = 4
-
-    def __init__(self):
-        n = ctypes.sizeof(_lib.WakeJob)
-        self.host = [torch.empty(n, dtype=torch.uint8, pin_memory=True) for _ in range(self.SLOTS)]
-        self.dev = [torch.empty(n, dtype=torch.uint8, device="cuda") for _ in range(self.SLOTS)]
-        self.event = [None] * self.SLOTS
-        self.stream = None
-        self.next = 0
-
-    def upload(self, job, stream):
-        if self.stream is not None and self.stream != stream.cuda_stream:
-            return jobs_to_device([job])
-        k = self.next
-        self.next = (k + 1) % self.SLOTS
-        if self.event[k] is not None:
-            self.event[k].synchronize()
-        ctypes.memmove(self.host[k].data_ptr(), ctypes.addressof(job), ctypes.sizeof(job))
-        with torch.cuda.stream(stream):
-            self.dev[k].copy_(self.host[k], non_blocking=True)
-            self.event[k] = torch.cuda.Event()
-            self.event[k].record(stream)
-        self.stream = stream.cuda_stream
-        return self.dev[k]
-
-
 class WakeEvaluator:
     """Runs the wake kernels over device observation points."""
 
@@ -130,6 +97,19 @@ class WakeEvaluator:
         xk = torch.empty(n, dtype=torch.float64, device=s.device)
         _lib.call("dfcsr_wake_fp64", ptr(jobs_dev), ptr(job_of_point), ptr(s), ptr(x), n, ptr(dE),
                   ptr(xk), stream_handle(stream))
+        return dE, xk
+
+    def mixed_job(self, job, s, x, xbins_max, zbins_max, use_band=False, stream=None):
+        """The mixed wake for one host WakeJob (passed by value: no job copy
+        on the stream)."""
+        n = s.numel()
+        dE = torch.empty(n, dtype=torch.float64, device=s.device)
+        xk = torch.empty(n, dtype=torch.float64, device=s.device)
+        need = _lib.query("dfcsr_wake_workspace_bytes", int(xbins_max), int(zbins_max), n)
+        buf = self.ws.get("wake", need)
+        _lib.call("dfcsr_wake_mixed_job", ctypes.byref(job), ptr(s), ptr(x), n, int(xbins_max),
+                  int(zbins_max), 1 if use_band else 0, ptr(dE), ptr(xk), ptr(buf), buf.numel(),
+                  stream_handle(stream))
         return dE, xk
 
     def mixed(self, jobs_dev, s, x, xbins_max, zbins_max, job_of_point=None, use_band=False,
@@ -203,7 +183,6 @@ class CSR2D:
         self.parallel = False
         self.evaluator = WakeEvaluator(workspace)
         self._jobs_dev = None
-        self._job_slot = None
         self._mesh = None
         self._mesh_host = None
         self._pending = None
@@ -317,16 +296,13 @@ class CSR2D:
         keeps the results on the device checks the DF finalisations with
         ``DF_tracker.check_status()`` when it next synchronises."""
         kind = self._wake_kind(precision)
-        if self._job_slot is None:
-            self._job_slot = _JobSlots()
-        jobs = self._job_slot.upload(self._job(),
-                                     stream if stream is not None else torch.cuda.current_stream())
-        self._jobs_dev = jobs
         ip = self.integration_params
         if kind == "fp64":
+            jobs = jobs_to_device([self._job()])
+            self._jobs_dev = jobs
             return self.evaluator.fp64(jobs, s, x, stream=stream)
-        return self.evaluator.mixed(jobs, s, x, ip.xbins, ip.zbins,
-                                    use_band=self.near_band > 0, stream=stream)
+        return self.evaluator.mixed_job(self._job(), s, x, ip.xbins, ip.zbins,
+                                        use_band=self.near_band > 0, stream=stream)
 
     def calculate_2D_CSR(self, precision=None, wait=True):
         """Wake on the whole observation mesh (CSR.py:397-418): sets

@@ -118,6 +118,8 @@ _SIGS = [
     ("dfcsr_deposit_cic2d_noalloc", _c_int, [_p, _p, _p, _p, _c_i64, _c_int, _c_double, _c_double,
                                               _c_int, _c_double, _c_double, _p, _p, _p]),
     ("dfcsr_df_workspace_bytes", _c_size, [_c_int, _c_int]),
+    ("dfcsr_df_axis_tables", _c_int, [_c_double, _c_double, _c_int, _c_double, _c_double, _c_int,
+                                       _c_int, _c_int, _p, _p, _p, _p, _p]),
     ("dfcsr_df_finalize", _c_int, [ctypes.POINTER(DFParams), _p, _p, _p, _p, _p, _p, _p,
                                     _c_size, _p]),
     ("dfcsr_grid_barrier_check", _c_int, [_c_int, _c_int, ctypes.c_uint, _p, _c_size, _p]),
@@ -134,6 +136,8 @@ _SIGS = [
     ("dfcsr_wake_workspace_bytes", _c_size, [_c_int, _c_int, _c_i64]),
     ("dfcsr_wake_mixed", _c_int, [_p, _p, _p, _p, _c_i64, _c_int, _c_int, _c_int, _p, _p, _p,
                                    _c_size, _p]),
+    ("dfcsr_wake_mixed_job", _c_int, [ctypes.POINTER(WakeJob), _p, _p, _c_i64, _c_int, _c_int,
+                                       _c_int, _p, _p, _p, _c_size, _p]),
     ("dfcsr_csr_mesh", _c_int, [_c_double, _c_double, _c_int, _c_double, _c_double, _c_int,
                                  _c_double, _c_double, _c_double, _p, _p, _p]),
     ("dfcsr_transport6", _c_int, [_p, _p, _c_i64, _c_i64, _p]),

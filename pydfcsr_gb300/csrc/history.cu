@@ -134,6 +134,51 @@ __global__ void rgi_axis_linspace(double s0, double s1, int ns, double t0, doubl
     oob[m] = (t < src.at(0) || t > src.at(ns - 1)) ? 1 : 0;
 }
 
+// get_DF's per-step axis tables (deposit.py:170-171, 212-213) from the grid
+// linspaces: diff(grid) and the coefficients numpy.gradient applies with a
+// coordinate array (edge_order 1) - per interior index a = -d2 / (d1 (d1 +
+// d2)), b = (d2 - d1) / (d1 d2), c = d1 / (d2 (d1 + d2)) with d1, d2 the
+// spacings below and above it; row 3 holds the first and last spacing (the
+// first twice when numpy takes its uniform-spacing branch).  Grid values by
+// numpy's linspace formula and the operations in numpy's order, so the
+// tables equal the host's bit for bit.  Thread t < nx handles x index t,
+// the next nz threads the z indices.
+__global__ void df_axis_tables(double x0, double x1, int nx, double z0, double z1, int nz,
+                               int x_uniform, int z_uniform, double *__restrict__ gx,
+                               double *__restrict__ gz, double *__restrict__ dxg,
+                               double *__restrict__ dzg) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nx + nz) return;
+    const bool onx = t < nx;
+    const Linspace L = onx ? Linspace(x0, x1, nx) : Linspace(z0, z1, nz);
+    const int n = onx ? nx : nz;
+    const int i = onx ? t : t - nx;
+    double *g = onx ? gx : gz;
+    double *d = onx ? dxg : dzg;
+    const int uniform = onx ? x_uniform : z_uniform;
+    const double gi = L.at(i);
+    if (i + 1 < n) d[i] = __dsub_rn(L.at(i + 1), gi);
+    double a = 0.0, b = 0.0, c = 0.0;
+    if (i >= 1 && i + 1 < n) {
+        const double d1 = __dsub_rn(gi, L.at(i - 1)), d2 = __dsub_rn(L.at(i + 1), gi);
+        const double s12 = __dadd_rn(d1, d2);
+        a = __ddiv_rn(-d2, __dmul_rn(d1, s12));
+        b = __ddiv_rn(__dsub_rn(d2, d1), __dmul_rn(d1, d2));
+        c = __ddiv_rn(d1, __dmul_rn(d2, s12));
+    }
+    g[i] = a;
+    g[n + i] = b;
+    g[2 * n + i] = c;
+    double r3 = 0.0;
+    if (n >= 2) {
+        const double first = __dsub_rn(L.at(1), L.at(0));
+        const double last = __dsub_rn(L.at(n - 1), L.at(n - 2));
+        if (i == 0) r3 = first;
+        else if (i == 1) r3 = uniform ? first : last;
+    }
+    g[3 * n + i] = r3;
+}
+
 }  // namespace dfcsr
 
 using namespace dfcsr;
@@ -180,6 +225,20 @@ extern "C" int dfcsr_history_regrid(const double *density, const double *density
         regrid5<false><<<blocks, 256, 0, as_stream(stream)>>>(
             density, density_x, density_z, vx, vx_x, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,
             vx_x_fill, ring64_slot, ring32_slot);
+    DFCSR_LAUNCH_CHECK();
+    return DFCSR_OK;
+}
+
+extern "C" int dfcsr_df_axis_tables(double x0, double x1, int nx, double z0, double z1, int nz,
+                                    int x_uniform, int z_uniform, double *gx, double *gz,
+                                    double *dxg, double *dzg, void *stream) {
+    clear_error();
+    DFCSR_CHECK_ARG(nx >= 2 && nz >= 2, "dfcsr_df_axis_tables: grids need >= 2 points (%d, %d)", nx, nz);
+    DFCSR_CHECK_ARG(gx && gz && dxg && dzg, "dfcsr_df_axis_tables: null pointer");
+    note_launch();
+    const int total = nx + nz;
+    df_axis_tables<<<(unsigned)((total + 127) / 128), 128, 0, as_stream(stream)>>>(
+        x0, x1, nx, z0, z1, nz, x_uniform ? 1 : 0, z_uniform ? 1 : 0, gx, gz, dxg, dzg);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }

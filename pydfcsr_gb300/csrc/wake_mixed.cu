@@ -1256,8 +1256,9 @@ static MixedLayout mixed_layout(int xbins_max, int zbins_max, int64_t n) {
 
 static size_t mixed_carve(Carver &c, const MixedLayout &L, unsigned long long **counter, float **rec,
                           PointMeta **meta, int2 **rows, double **part, double **band,
-                          double **obs_vx, GeoShared **setup) {
+                          double **obs_vx, GeoShared **setup, dfcsr_wake_job **jobslot) {
     *counter = c.take<unsigned long long>(4);
+    *jobslot = c.take<dfcsr_wake_job>(1);
     *setup = c.take<GeoShared>((size_t)L.setup_pts);
     *rec = c.take<float>((size_t)L.batch * L.rec_words);
     *meta = c.take<PointMeta>((size_t)L.batch);
@@ -1320,17 +1321,27 @@ extern "C" size_t dfcsr_wake_workspace_bytes(int xbins_max, int zbins_max, int64
     int2 *rw;
     double *p, *q, *v;
     GeoShared *g;
-    return mixed_carve(c, L, &a, &b, &m, &rw, &p, &q, &v, &g) + 256;
+    dfcsr_wake_job *j;
+    return mixed_carve(c, L, &a, &b, &m, &rw, &p, &q, &v, &g, &j) + 256;
 }
 
-extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
-                                const double *s, const double *x, int64_t n, int xbins_max,
-                                int zbins_max, int use_band, double *dE, double *xkick,
-                                void *workspace, size_t workspace_bytes, void *stream) {
-    clear_error();
+namespace dfcsr {
+// One job passed by value (a kernel parameter) into its workspace slot.
+__global__ void store_job(dfcsr_wake_job job, dfcsr_wake_job *__restrict__ out) {
+    if (threadIdx.x == 0) *out = job;
+}
+}  // namespace dfcsr
+
+// The mixed wake over n points: jobs in device memory (`jobs`, with
+// `job_of_point`), or one job from host memory (`job_host`), stored into the
+// workspace by the first kernel of the stream.
+static int wake_mixed_run(const dfcsr_wake_job *jobs, const dfcsr_wake_job *job_host,
+                          const int32_t *job_of_point, const double *s, const double *x, int64_t n,
+                          int xbins_max, int zbins_max, int use_band, double *dE, double *xkick,
+                          void *workspace, size_t workspace_bytes, void *stream) {
     DFCSR_CHECK_ARG(n >= 0, "dfcsr_wake_mixed: negative point count");
     if (n == 0) return DFCSR_OK;
-    DFCSR_CHECK_ARG(jobs && s && x && dE && xkick, "dfcsr_wake_mixed: null pointer");
+    DFCSR_CHECK_ARG((jobs || job_host) && s && x && dE && xkick, "dfcsr_wake_mixed: null pointer");
     DFCSR_CHECK_ARG(xbins_max >= 1 && 2 * xbins_max <= MX_MAX_ROWS,
                     "dfcsr_wake_mixed: xbins must be in [1, %d] (got %d)", MX_MAX_ROWS / 2, xbins_max);
     DFCSR_CHECK_ARG(zbins_max >= 1 && zbins_max <= MX_MAX_COLS,
@@ -1343,12 +1354,19 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
     int2 *rows;
     double *part, *band, *obs_vx;
     GeoShared *setup;
-    mixed_carve(c, L, &counter, &rec, &meta, &rows, &part, &band, &obs_vx, &setup);
+    dfcsr_wake_job *jobslot;
+    mixed_carve(c, L, &counter, &rec, &meta, &rows, &part, &band, &obs_vx, &setup, &jobslot);
     if (!workspace || !c.ok()) {
         set_error("dfcsr_wake_mixed: workspace too small (%zu < %zu)", workspace_bytes, c.used);
         return DFCSR_OOM;
     }
     cudaStream_t st = as_stream(stream);
+    if (job_host) {
+        note_launch();
+        store_job<<<1, 32, 0, st>>>(*job_host, jobslot);
+        jobs = jobslot;
+        job_of_point = nullptr;
+    }
     const int max_rows = 2 * xbins_max;
     const size_t smem = integral_smem_bytes(max_rows);
     int blocks_max = 0;
@@ -1393,4 +1411,24 @@ extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_o
     }
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
+}
+
+extern "C" int dfcsr_wake_mixed(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
+                                const double *s, const double *x, int64_t n, int xbins_max,
+                                int zbins_max, int use_band, double *dE, double *xkick,
+                                void *workspace, size_t workspace_bytes, void *stream) {
+    clear_error();
+    DFCSR_CHECK_ARG(n == 0 || jobs, "dfcsr_wake_mixed: null pointer");
+    return wake_mixed_run(jobs, nullptr, job_of_point, s, x, n, xbins_max, zbins_max, use_band, dE,
+                          xkick, workspace, workspace_bytes, stream);
+}
+
+extern "C" int dfcsr_wake_mixed_job(const dfcsr_wake_job *job, const double *s, const double *x,
+                                    int64_t n, int xbins_max, int zbins_max, int use_band, double *dE,
+                                    double *xkick, void *workspace, size_t workspace_bytes,
+                                    void *stream) {
+    clear_error();
+    DFCSR_CHECK_ARG(n == 0 || job, "dfcsr_wake_mixed_job: null job");
+    return wake_mixed_run(nullptr, job, nullptr, s, x, n, xbins_max, zbins_max, use_band, dE, xkick,
+                          workspace, workspace_bytes, stream);
 }

@@ -25,7 +25,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .coeffs import gradient_table, savgol_tables
+from .coeffs import savgol_tables
 from .runtime import (as_device_f64, default_workspace, host_to_device, ptr, require_cuda,
                       stream_handle)
 
@@ -91,8 +91,12 @@ def deposit_cic_from_moments(q1, q2, w0, w1, nbins_1, nbins_2, moments, lim_1, l
         out1 = torch.empty((nb1, nb2), dtype=torch.float64, device=q1.device)
     need = _lib.query("dfcsr_deposit_workspace_bytes", n, nb1, nb2)
     buf = ws.get("deposit", need)
+    m = moments.contiguous()
+    # the deposit's first kernel reads the moments on `stream`: keep their
+    # memory from being reused by the allocator before it has run
+    m.record_stream(stream if stream is not None else torch.cuda.current_stream())
     _lib.call("dfcsr_deposit_cic2d_moments", ptr(q1), ptr(q2), ptr(w0), ptr(w1), n, nb1, nb2,
-              ptr(moments.contiguous()), float(lim_1), float(lim_2), ptr(out0), ptr(out1),
+              ptr(m), float(lim_1), float(lim_2), ptr(out0), ptr(out1),
               ptr(buf), buf.numel(), stream_handle(stream))
     return out0, out1
 
@@ -196,6 +200,27 @@ class HistoryRing:
         if self.ring64 is not None:
             return self.ring64[idx][..., f].cpu().numpy()
         return self.ring32[idx][..., f].double().cpu().numpy()
+
+
+_SG_DEVICE = {}
+
+
+def _sg_tables_device(window, order):
+    """Savitzky-Golay tables (coeff, lo, hi of coeffs.savgol_tables) in device
+    memory, one copy per device and (window, order), uploaded once with a
+    blocking copy (so any stream may read them).  Returns (tensor, (coeff,
+    lo, hi) device addresses)."""
+    dev = torch.cuda.current_device()
+    key = (dev, window, order)
+    hit = _SG_DEVICE.get(key)
+    if hit is None:
+        coeff, lo, hi = savgol_tables(window, order)
+        parts = [coeff, lo.ravel(), hi.ravel()]
+        t = torch.from_numpy(np.concatenate(parts)).to(torch.device("cuda", dev))
+        offs = np.concatenate([[0], np.cumsum([p.size for p in parts])])
+        hit = (t, tuple(t.data_ptr() + 8 * int(o) for o in offs[:3]))
+        _SG_DEVICE[key] = hit
+    return hit
 
 
 class PendingDeposit:
@@ -395,36 +420,44 @@ class DF_tracker:
         xg = np.linspace(x0, x1, xb)
         zg = np.linspace(z0, z1, zb)
         sc = torch.empty(8, dtype=torch.float64, device=fields.device)   # written by df_finalize
-        self._finalize(fields, sc, xg, zg, win, stream, ws)
+        self._finalize(fields, sc, (x0, x1, xb), (z0, z1, zb), xg, zg, win, stream, ws)
         self.x_grids, self.z_grids = xg, zg
         self._cur = _DFEntry(xg, zg, fields, sc, t, sigma_x, sigma_z, (x0, x1, xb), (z0, z1, zb))
         self.t = t
         self.bins = (xb, zb, win)
 
-    def _finalize(self, fields, sc, xg, zg, win, stream, ws):
+    def _finalize(self, fields, sc, xlin, zlin, xg, zg, win, stream, ws):
+        """The DF stage on the deposited fields.  The Savitzky-Golay tables
+        come from a per-device cache; the grid tables (numpy.gradient
+        coefficients and diff of each grid) are computed on the device from
+        the two linspaces (``dfcsr_df_axis_tables``), equal to the host's
+        ``coeffs.gradient_table`` bit for bit; the host only decides numpy's
+        uniform-spacing branch from ``xg`` and ``zg``."""
         xb, zb = xg.size, zg.size
-        coeff, lo, hi = savgol_tables(win, int(self.filter_order))
-        gx, gxu, gxdx = gradient_table(xg)
-        gz, gzu, gzdx = gradient_table(zg)
-        # one host->device copy of all per-step constants
-        parts = [coeff, lo.ravel(), hi.ravel(), gx.ravel(), gz.ravel(), np.diff(xg), np.diff(zg)]
-        sizes = [p.size for p in parts]
-        blob = host_to_device(np.concatenate(parts))
-        offs = np.concatenate([[0], np.cumsum(sizes)])
-        base = blob.data_ptr()
+        sg = _sg_tables_device(int(win), int(self.filter_order))
+        dxh, dzh = np.diff(xg), np.diff(zg)
+        gxu, gzu = bool(np.all(dxh == dxh[0])), bool(np.all(dzh == dzh[0]))
+        sizes = [4 * xb, 4 * zb, xb - 1, zb - 1]
+        offs = np.concatenate([[0], np.cumsum([(v + 31) // 32 * 32 for v in sizes])])
+        tab = ws.get("df_axes", 8 * int(offs[-1]))
+        base = tab.data_ptr()
+        gx, gz, dxg, dzg = [base + 8 * int(o) for o in offs[:4]]
+        _lib.call("dfcsr_df_axis_tables", float(xlin[0]), float(xlin[1]), xb, float(zlin[0]),
+                  float(zlin[1]), zb, int(gxu), int(gzu), ctypes.c_void_p(gx), ctypes.c_void_p(gz),
+                  ctypes.c_void_p(dxg), ctypes.c_void_p(dzg), stream_handle(stream))
         P = _lib.DFParams()
         P.nx, P.nz, P.window, P.order = xb, zb, int(win), int(self.filter_order)
         P.velocity_threshold = float(self.velocity_threhold)
-        (P.sg_coeff, P.sg_lo, P.sg_hi, P.gx, P.gz, P.dxg, P.dzg) = [base + 8 * int(o) for o in offs[:7]]
+        P.sg_coeff, P.sg_lo, P.sg_hi = sg[1]
+        P.gx, P.gz, P.dxg, P.dzg = gx, gz, dxg, dzg
         P.gx_uniform, P.gz_uniform = int(gxu), int(gzu)
-        P.gx_dx, P.gz_dx = gxdx, gzdx
+        P.gx_dx, P.gz_dx = float(dxh[0]), float(dzh[0])
         P.barrier_spins, P.barrier_extra = int(self.barrier_spins), int(self.barrier_extra)
         need = _lib.query("dfcsr_df_workspace_bytes", xb, zb)
         buf = ws.get("df", need)
         _lib.call("dfcsr_df_finalize", ctypes.byref(P), ptr(fields[0]), ptr(fields[3]),
                   ptr(fields[1]), ptr(fields[2]), ptr(fields[4]), ptr(sc), ptr(buf), buf.numel(),
                   stream_handle(stream))
-        self._blob = blob   # keep the constants alive until the stream consumes them
         ev = torch.cuda.Event()
         ev.record(stream if stream is not None else torch.cuda.current_stream())
         self._unchecked.append((sc, ev))

@@ -53,57 +53,15 @@ def as_device_f64(a, device=None):
     return _async_upload(arr, dev)
 
 
-class _PinnedRing:
-    """Reusable pinned staging buffers for small host->device uploads (the
-    per-step tables, grids and job structs): a slot's buffer is rewritten
-    once the copy out of it has run (its event; SLOTS uploads earlier, long
-    past in a step loop).  Saves the pinned allocation and registration of a
-    fresh staging tensor per upload."""
-    SLOTS = 16
-    MAX_BYTES = 1 << 20
-
-    def __init__(self):
-        self.bufs = [None] * self.SLOTS
-        self.events = [None] * self.SLOTS
-        self.k = 0
-
-    def upload(self, t, dev):
-        k = self.k
-        self.k = (k + 1) % self.SLOTS
-        if self.events[k] is not None:
-            self.events[k].synchronize()
-        nbytes = t.numel() * t.element_size()
-        buf = self.bufs[k]
-        if buf is None or buf.numel() < nbytes:
-            buf = torch.empty(max(nbytes, 4096), dtype=torch.uint8, pin_memory=True)
-            self.bufs[k] = buf
-        stage = buf[:nbytes].view(t.dtype).view(t.shape)
-        stage.copy_(t)
-        out = torch.empty(t.shape, dtype=t.dtype, device=dev)
-        out.copy_(stage, non_blocking=True)
-        ev = torch.cuda.Event()
-        ev.record(torch.cuda.current_stream(dev))
-        self.events[k] = ev
-        return out
-
-
-_rings = {}
-
-
 def _async_upload(a, dev):
-    """Copy a host array to the device without blocking the host: small
-    arrays through a ring of reusable pinned buffers, larger ones through
-    torch's caching pinned-host allocator (which keeps the staging block
-    alive until the copy has run on the current stream)."""
+    """Stage through torch's caching pinned-host allocator and copy without
+    blocking the host; the allocator keeps the staging block alive until the
+    copy has run on the current stream.  (A ring of reusable pinned buffers
+    with an event per slot measured slower on the host: 43 vs 21 us per
+    small upload.)"""
     t = torch.from_numpy(a)
     if t.numel() == 0:
         return t.to(dev)
-    if t.numel() * t.element_size() <= _PinnedRing.MAX_BYTES:
-        idx = dev.index if dev.index is not None else torch.cuda.current_device()
-        ring = _rings.get(idx)
-        if ring is None:
-            ring = _rings[idx] = _PinnedRing()
-        return ring.upload(t, torch.device("cuda", idx))
     return t.pin_memory().to(dev, non_blocking=True)
 
 

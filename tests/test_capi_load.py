@@ -93,6 +93,14 @@ def test_bad_arguments_fail_without_gpu():
                   ctypes.c_void_p(16), 5, 2000, 100, 0, ctypes.c_void_p(16), ctypes.c_void_p(16),
                   None, 0, None)
     assert "xbins" in _lib.load().dfcsr_last_error().decode()
+    job = _lib.WakeJob()
+    with pytest.raises(_lib.DfcsrBadArgument, match="xbins"):
+        _lib.call("dfcsr_wake_mixed_job", ctypes.byref(job), ctypes.c_void_p(16),
+                  ctypes.c_void_p(16), 5, 2000, 100, 0, ctypes.c_void_p(16), ctypes.c_void_p(16),
+                  None, 0, None)
+    with pytest.raises(_lib.DfcsrBadArgument, match="null job"):
+        _lib.call("dfcsr_wake_mixed_job", None, ctypes.c_void_p(16), ctypes.c_void_p(16), 5, 100,
+                  100, 0, ctypes.c_void_p(16), ctypes.c_void_p(16), None, 0, None)
     with pytest.raises(_lib.DfcsrBadArgument, match="extra_arrivals"):
         _lib.call("dfcsr_grid_barrier_check", 1, 2, 100, ctypes.c_void_p(16), 16, None)
     with pytest.raises(_lib.DfcsrBadArgument, match="workspace"):

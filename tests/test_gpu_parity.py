@@ -236,6 +236,11 @@ def test_wake_mixed_geometry_paths(tag):
         assert max(e.values()) <= 1e-4, (path, e)
     e = wake_errors(*out["fp64"], *out["dw"])
     assert e["max_rel"] < 1e-6, e
+    # the same job passed by value (dfcsr_wake_mixed_job, what wake_device
+    # uses) gives the device-job result bit for bit
+    dE, xk = csr.evaluator.mixed_job(csr._job(), s, x, ip.xbins, ip.zbins)
+    assert np.array_equal(dE.cpu().numpy(), out["dw"][0])
+    assert np.array_equal(xk.cpu().numpy(), out["dw"][1])
 
 
 @cuda
@@ -354,9 +359,39 @@ def test_calculate_2d_csr_nonblocking_matches_blocking():
     assert np.array_equal(dE0, dE1) and np.array_equal(xk0, xk1)
     csr.calculate_2D_CSR("mixed", wait=False)
     assert np.array_equal(csr.dE_dct, dE0) and np.array_equal(csr.x_kick, xk0)
-    # the library's launch counter sees the mesh kernel and the wake's set-up,
-    # geometry, integral and finalize launches (one batch here)
+    # the library's launch counter sees the mesh kernel and the wake's job
+    # store, set-up, geometry, integral and finalize launches (one batch here)
     from pydfcsr_gb300 import _lib
     n0 = _lib.kernel_launches()
     csr.calculate_2D_CSR("mixed")
-    assert _lib.kernel_launches() - n0 == 5
+    assert _lib.kernel_launches() - n0 == 6
+
+
+@cuda
+@pytest.mark.parametrize("x0,x1,nx,z0,z1,nz", [
+    (0.0, 1.0, 5, -2.0, 2.0, 9),                    # exact spacings: numpy's uniform branch
+    (-1.07e-4, 1.31e-4, 256, -2.6e-4, 2.2e-4, 256),  # spacings that differ by an ulp
+    (3.3e-5, 9.1e-5, 2, -5e-5, 5e-5, 513),
+])
+def test_df_axis_tables_match_numpy(x0, x1, nx, z0, z1, nz):
+    """dfcsr_df_axis_tables against coeffs.gradient_table (numpy.gradient's
+    coefficients) and numpy.diff on the host's linspace grids: bit for bit."""
+    import ctypes
+    import torch
+    from pydfcsr_gb300 import _lib
+    from pydfcsr_gb300.coeffs import gradient_table
+    from pydfcsr_gb300.runtime import stream_handle
+    xg, zg = np.linspace(x0, x1, nx), np.linspace(z0, z1, nz)
+    gxh, gxu, _ = gradient_table(xg)
+    gzh, gzu, _ = gradient_table(zg)
+    gx = torch.full((4, nx), np.nan, dtype=torch.float64, device="cuda")
+    gz = torch.full((4, nz), np.nan, dtype=torch.float64, device="cuda")
+    dx = torch.full((max(nx - 1, 1),), np.nan, dtype=torch.float64, device="cuda")
+    dz = torch.full((nz - 1,), np.nan, dtype=torch.float64, device="cuda")
+    _lib.call("dfcsr_df_axis_tables", x0, x1, nx, z0, z1, nz, int(gxu), int(gzu),
+              ctypes.c_void_p(gx.data_ptr()), ctypes.c_void_p(gz.data_ptr()),
+              ctypes.c_void_p(dx.data_ptr()), ctypes.c_void_p(dz.data_ptr()), stream_handle())
+    assert np.array_equal(gx.cpu().numpy(), gxh)
+    assert np.array_equal(gz.cpu().numpy(), gzh)
+    assert np.array_equal(dx.cpu().numpy()[:nx - 1], np.diff(xg))
+    assert np.array_equal(dz.cpu().numpy(), np.diff(zg))
