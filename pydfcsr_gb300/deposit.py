@@ -26,8 +26,7 @@ import torch
 
 from . import _lib
 from .coeffs import savgol_tables
-from .runtime import (as_device_f64, default_workspace, host_to_device, ptr, require_cuda,
-                      stream_handle)
+from .runtime import as_device_f64, default_workspace, ptr, require_cuda, stream_handle
 
 __all__ = ["histogram_cic_2d", "deposit_cic", "beam_moments", "DF_tracker", "HistoryRing",
            "FIELDS"]
