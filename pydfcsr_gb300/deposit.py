@@ -536,8 +536,11 @@ class DF_tracker:
         pad = lambda b: (b + 255) // 256 * 256
         sizes = [pad(8 * nxi), pad(8 * nzi), pad(4 * nxi), pad(4 * nzi), pad(nxi), pad(nzi)]
         buf = self._workspace().get("rgi", sum(sizes))
-        offs = np.concatenate([[0], np.cumsum(sizes)])
-        wx, wz, ix, iz, ox, oz = (ctypes.c_void_p(buf.data_ptr() + int(o)) for o in offs[:6])
+        key = (buf.data_ptr(), nxi, nzi)
+        if getattr(self, "_rgi_ptrs", (None,))[0] != key:   # table pointers, once per buffer
+            offs = np.concatenate([[0], np.cumsum(sizes)])
+            self._rgi_ptrs = (key, tuple(ctypes.c_void_p(buf.data_ptr() + int(o)) for o in offs[:6]))
+        wx, wz, ix, iz, ox, oz = self._rgi_ptrs[1]
         h = stream_handle(stream)
         _lib.call("dfcsr_rgi_axis_linspace", xs0, xs1, xsn, xt0, xt1, nxi, ix, wx, ox, h)
         _lib.call("dfcsr_rgi_axis_linspace", zs0, zs1, zsn, zt0, zt1, nzi, iz, wz, oz, h)
