@@ -218,18 +218,23 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
     const dw xref = gs.xrefw[r];
     const dw rx0 = dw_sub(dw_sub(gs.Px, L[0]), dw_mul(xref, npx));
     const dw ry0 = dw_sub(dw_sub(gs.Py, L[1]), dw_mul(xref, npy));
-    const dw r0 = dw_sqrt(dw_add(dw_mul(rx0, rx0), dw_mul(ry0, ry0)));
+    const dw r0 = dw_sqrt(dw_add_abs(dw_mul(rx0, rx0), dw_mul(ry0, ry0)));   // both >= 0
     const dw ut0 = dw_mul(dw_sub(gs.T0, r0), gs.inv_t);
     const dw uz0 = dw_mul(dw_add(dw_sub(spj, gs.Tz), r0), gs.inv_z);
     const float tfl = dw_floor(ut0), zfl = dw_floor(uz0);
-    const dw a = dw_add(dw_mul(vxo, tpx), dw_mul(vyo, tpy));
-    const dw bb = dw_add(dw_mul(vxo, npx), dw_mul(vyo, npy));
-    const dw e = dw_add(dw_mul(tpx, npx), dw_mul(tpy, npy));
-    const dw g = dw_add(dw_mul(npx, npx), dw_mul(npy, npy));
-    const dw h = dw_add(dw_mul(tpx, tpx), dw_mul(tpy, tpy));
+    // dot products of the orbit vectors: sums of two products whose
+    // absolute error 2^-48 (|x| + |y|) is far below what the integrand reads
+    // from them (unit vectors: a cancellation leaves a small value, not a
+    // small relative error that matters); position differences (rx0, ry0
+    // above, the history coordinates) keep the accurate double-word sum
+    const dw a = dw_add_abs(dw_mul(vxo, tpx), dw_mul(vyo, tpy));
+    const dw bb = dw_add_abs(dw_mul(vxo, npx), dw_mul(vyo, npy));
+    const dw e = dw_add_abs(dw_mul(tpx, npx), dw_mul(tpy, npy));
+    const dw g = dw_add_abs(dw_mul(npx, npx), dw_mul(npy, npy));
+    const dw h = dw_add_abs(dw_mul(tpx, tpx), dw_mul(tpy, tpy));
     const dw nmx = dw_sub(gs.nsx, npx), nmy = dw_sub(gs.nsy, npy);
-    const dw Q0 = dw_add(dw_mul(rx0, nmx), dw_mul(ry0, nmy));
-    const dw q2 = dw_add(dw_mul(gs.nsx, tpx), dw_mul(gs.nsy, tpy));
+    const dw Q0 = dw_add_abs(dw_mul(rx0, nmx), dw_mul(ry0, nmy));
+    const dw q2 = dw_add_abs(dw_mul(gs.nsx, tpx), dw_mul(gs.nsy, tpy));
     const dw ae = dw_mul(a, e);
     float rho_f;
     if (gs.nthr[r] >= 0) {
@@ -241,8 +246,8 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
     }
     const bool near = gs.band_f > 0.f && fabsf(dw_float(dw_sub(spj, gs.Sw))) < gs.band_f;
     const float ws = (j == 0 || j == gs.ax_s[r].n - 1) ? gs.wsf[r][0] : gs.wsf[r][1];
-    const dw R0n = dw_add(dw_mul(rx0, npx), dw_mul(ry0, npy));
-    const dw cr = dw_sub(dw_mul(rx0, npy), dw_mul(ry0, npx));
+    const dw R0n = dw_add_abs(dw_mul(rx0, npx), dw_mul(ry0, npy));
+    const dw cr = dw_sub_abs(dw_mul(rx0, npy), dw_mul(ry0, npx));
     const dw us = dw_div(R0n, g);
     const dw rmin2 = dw_div(dw_mul(cr, cr), g);
     const dw toff = dw_add_f(ut0, -tfl), zoff = dw_add_f(uz0, -zfl);
@@ -253,11 +258,11 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
     o[2] = make_float4(us.hi, us.lo, rmin2.hi, rmin2.lo);
     o[3] = make_float4(dw_float(dw_add_f(g, -1.f)), K0x.hi, K0x.lo, rho_f);
     o[4] = make_float4(dw_float(a), dw_float(bb), dw_float(e), dw_float(h));
-    o[5] = make_float4(dw_float(dw_add(dw_add_f(dw_mul(a, g), -1.f), dw_mul(bb, e))),
+    o[5] = make_float4(dw_float(dw_add_abs(dw_add_f(dw_mul(a, g), -1.f), dw_mul(bb, e))),
                        dw_float(dw_mul(bb, g)), dw_float(dw_mul(a, dw_add_f(dw_neg(h), 1.f))),
-                       dw_float(dw_add(ae, dw_mul(bb, h))));
+                       dw_float(dw_add_abs(ae, dw_mul(bb, h))));
     o[6] = make_float4(dw_float(dw_mul(bb, e)), dw_float(Q0),
-                       dw_float(dw_add(dw_mul(npx, nmx), dw_mul(npy, nmy))), dw_float(q2));
+                       dw_float(dw_add_abs(dw_mul(npx, nmx), dw_mul(npy, nmy))), dw_float(q2));
     o[7] = make_float4(dw_float(dw_sub(Q0, dw_mul(q2, r0))), near ? 0.f : ws,
                        __fsub_rn(a.hi, dw_float(a)) + a.lo, 0.f);   // band columns: FP64 kernel
     o[8] = make_float4(0.f, 0.f, 0.f, 0.f);
