@@ -101,6 +101,18 @@ def test_bad_arguments_fail_without_gpu():
     with pytest.raises(_lib.DfcsrBadArgument, match="null job"):
         _lib.call("dfcsr_wake_mixed_job", None, ctypes.c_void_p(16), ctypes.c_void_p(16), 5, 100,
                   100, 0, ctypes.c_void_p(16), ctypes.c_void_p(16), None, 0, None)
+    with pytest.raises(_lib.DfcsrBadArgument, match="grids need"):
+        _lib.call("dfcsr_df_axis_tables", 0.0, 1.0, 1, 0.0, 1.0, 8, 0, 0, ctypes.c_void_p(16),
+                  ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16), None)
+    with pytest.raises(_lib.DfcsrBadArgument, match="moments is null"):
+        _lib.call("dfcsr_deposit_cic2d_moments", ctypes.c_void_p(16), ctypes.c_void_p(16), None,
+                  None, 10, 8, 8, None, 5.0, 5.0, ctypes.c_void_p(16), None, None, 0, None)
+    with pytest.raises(_lib.DfcsrBadArgument, match="limits"):
+        _lib.call("dfcsr_deposit_cic2d_moments", ctypes.c_void_p(16), ctypes.c_void_p(16), None,
+                  None, 10, 8, 8, ctypes.c_void_p(16), 0.0, 5.0, ctypes.c_void_p(16), None, None,
+                  0, None)
+    # an empty wake is a no-op, with or without a job
+    _lib.call("dfcsr_wake_mixed_job", None, None, None, 0, 100, 100, 0, None, None, None, 0, None)
     with pytest.raises(_lib.DfcsrBadArgument, match="extra_arrivals"):
         _lib.call("dfcsr_grid_barrier_check", 1, 2, 100, ctypes.c_void_p(16), 16, None)
     with pytest.raises(_lib.DfcsrBadArgument, match="workspace"):
