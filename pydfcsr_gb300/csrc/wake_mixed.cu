@@ -951,6 +951,9 @@ struct ChunkSums {
 #define MX_INTEGRAL_ROWBLK 4
 #endif
 constexpr int MX_ROWBLK = MX_INTEGRAL_ROWBLK;
+#ifndef MX_DXDW_REGIONS
+#define MX_DXDW_REGIONS 2
+#endif
 
 template <bool DXDW>
 __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float4 *__restrict__ rows,
@@ -1127,9 +1130,9 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
                     for (int k = tid; k < C * (CW / 4); k += blockDim.x) sm.col[k] = cb[k];
                     __syncthreads();
                     ChunkSums acc{dw{0.f, 0.f}, 0.f, 0.f, 0.f, 0.f};
-                    // regions 0 and 1 (far and middle): density_x's terms
-                    // cancel to ~1/300 of their size there
-                    if (r < 2)
+                    // regions below MX_DXDW_REGIONS (0 far, 1 middle):
+                    // density_x's terms cancel to ~1/300 of their size there
+                    if (r < MX_DXDW_REGIONS)
                         chunk_points<true>(sm, rows, V, rv.x, rv.y, C, acc);
                     else
                         chunk_points<false>(sm, rows, V, rv.x, rv.y, C, acc);
