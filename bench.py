@@ -855,7 +855,7 @@ def roofline(kname, launch_ms, launches, per_obs_total, npts, fma_peaks, hbm, pr
 
 
 # From an ncu capture of wake_mixed_integral on this workload at a 4-region
-# step (profiles/wake_mixed_integral_chicane.md, 2.048e8 integrand points):
+# step (the ncu --set full capture of step 40's launch, 2.048e8 integrand points):
 # FP32 operations per integrand point from the executed (predicated-on)
 # thread instructions (23.28e9 FADD + 3.11e9 FMUL + 2 x 5.89e9 FFMA), DRAM
 # bytes per integrand point (345.8 + 4.3 MB), warp instructions per
