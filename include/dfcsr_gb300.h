@@ -303,9 +303,13 @@ typedef struct {
 
 /* Plain FP64 drop-in: reproduces the reference's IEEE operation order
  * (trapz over x' summed row by row, then numpy pairwise over s').  Needs
- * ring64.  Outputs dE[n], xkick[n] (MeV/m). */
+ * ring64.  zbins_max: the largest integration zbins (s' columns per
+ * region) of the jobs in the call, 1..6144 (up to 1024 the column sums sit
+ * in static shared memory; above, in dynamic shared memory sized to
+ * zbins_max).  A job whose zbins exceeds zbins_max gets NaN.  Outputs
+ * dE[n], xkick[n] (MeV/m). */
 int dfcsr_wake_fp64(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
-                    const double *s, const double *x, int64_t n,
+                    const double *s, const double *x, int64_t n, int zbins_max,
                     double *dE, double *xkick, void *stream);
 
 /* Observation points of get_CSR_mesh + calculate_2D_CSR (CSR.py:361-418):

@@ -91,12 +91,12 @@ class WakeEvaluator:
     def __init__(self, workspace=None):
         self.ws = workspace or default_workspace()
 
-    def fp64(self, jobs_dev, s, x, job_of_point=None, stream=None):
+    def fp64(self, jobs_dev, s, x, zbins_max, job_of_point=None, stream=None):
         n = s.numel()
         dE = torch.empty(n, dtype=torch.float64, device=s.device)
         xk = torch.empty(n, dtype=torch.float64, device=s.device)
-        _lib.call("dfcsr_wake_fp64", ptr(jobs_dev), ptr(job_of_point), ptr(s), ptr(x), n, ptr(dE),
-                  ptr(xk), stream_handle(stream))
+        _lib.call("dfcsr_wake_fp64", ptr(jobs_dev), ptr(job_of_point), ptr(s), ptr(x), n,
+                  int(zbins_max), ptr(dE), ptr(xk), stream_handle(stream))
         return dE, xk
 
     def mixed_job(self, job, s, x, xbins_max, zbins_max, use_band=False, stream=None):
@@ -300,7 +300,7 @@ class CSR2D:
         if kind == "fp64":
             jobs = jobs_to_device([self._job()])
             self._jobs_dev = jobs
-            return self.evaluator.fp64(jobs, s, x, stream=stream)
+            return self.evaluator.fp64(jobs, s, x, ip.zbins, stream=stream)
         return self.evaluator.mixed_job(self._job(), s, x, ip.xbins, ip.zbins,
                                         use_band=self.near_band > 0, stream=stream)
 

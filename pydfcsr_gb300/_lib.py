@@ -130,7 +130,7 @@ _SIGS = [
     ("dfcsr_interp3d", _c_int, [_p, _p, _p, _c_i64, _p, _c_int, _c_int, _c_int, _c_double,
                                  _c_double, _c_double, _c_double, _c_double, _c_double, _p, _p]),
     ("dfcsr_interp1d", _c_int, [_p, _c_i64, _p, _c_int, _c_double, _c_double, _p, _p]),
-    ("dfcsr_wake_fp64", _c_int, [_p, _p, _p, _p, _c_i64, _p, _p, _p]),
+    ("dfcsr_wake_fp64", _c_int, [_p, _p, _p, _p, _c_i64, _c_int, _p, _p, _p]),
     ("dfcsr_wake_integrand", _c_int, [_p, _c_double, _c_double, _p, _p, _c_i64, _c_int, _p, _p,
                                        _p]),
     ("dfcsr_wake_workspace_bytes", _c_size, [_c_int, _c_int, _c_i64]),

@@ -8,19 +8,28 @@
 // column and sums its x' terms row by row (numpy reduces axis 0 of a C array
 // sequentially); the column integrals are then added with numpy's pairwise
 // summation.  One CTA evaluates one observation point.
+#include <mutex>
+
 #include "wake_common.cuh"
 
 namespace dfcsr {
 
 constexpr int F64_THREADS = 128;
-constexpr int F64_MAX_COLS = 1024;
+// s' columns per region: up to F64_STATIC_COLS in static shared memory (the
+// usual case, three CTAs per SM); up to F64_MAX_COLS in dynamic shared
+// memory sized to the call's zbins (4 arrays of 8 B per column).
+constexpr int F64_STATIC_COLS = 1024;
+constexpr int F64_MAX_COLS = 6144;
 
+template <bool DYN>
 __global__ void __launch_bounds__(F64_THREADS)
 wake_fp64_kernel(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__ job_of_point,
                  const double *__restrict__ S, const double *__restrict__ X, int64_t n,
-                 double *__restrict__ dE, double *__restrict__ xkick) {
-    __shared__ double colz[F64_MAX_COLS], colx[F64_MAX_COLS];
-    __shared__ double tz[F64_MAX_COLS], tx[F64_MAX_COLS];
+                 int cols_cap, double *__restrict__ dE, double *__restrict__ xkick) {
+    __shared__ double s_cols[DYN ? 1 : 4 * F64_STATIC_COLS];
+    extern __shared__ double d_cols[];
+    double *colz = DYN ? d_cols : s_cols;
+    double *colx = colz + cols_cap, *tz = colx + cols_cap, *tx = tz + cols_cap;
     __shared__ double red[2];
     for (int64_t pt = blockIdx.x; pt < n; pt += gridDim.x) {
         const dfcsr_wake_job &J = jobs[job_of_point ? job_of_point[pt] : 0];
@@ -39,7 +48,7 @@ wake_fp64_kernel(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restr
         bool bad = false;
         for (int r = 0; r < nreg; ++r) {
             const Region R = reg[r];
-            if (R.nsp < 1 || R.nsp > F64_MAX_COLS || R.nxp < 1) { bad = true; break; }
+            if (R.nsp < 1 || R.nsp > cols_cap || R.nxp < 1) { bad = true; break; }
             for (int j = threadIdx.x; j < R.nsp; j += blockDim.x) {
                 const double spj = np_linspace_at(R.sl, R.sr, R.nsp, j);
                 double lat_sp[6];
@@ -133,17 +142,43 @@ extern "C" int dfcsr_wake_integrand(const dfcsr_wake_job *job, double s, double 
 }
 
 extern "C" int dfcsr_wake_fp64(const dfcsr_wake_job *jobs, const int32_t *job_of_point,
-                               const double *s, const double *x, int64_t n, double *dE,
-                               double *xkick, void *stream) {
+                               const double *s, const double *x, int64_t n, int zbins_max,
+                               double *dE, double *xkick, void *stream) {
     clear_error();
     DFCSR_CHECK_ARG(n >= 0, "dfcsr_wake_fp64: negative point count");
     if (n == 0) return DFCSR_OK;
     DFCSR_CHECK_ARG(jobs && s && x && dE && xkick, "dfcsr_wake_fp64: null pointer");
+    DFCSR_CHECK_ARG(zbins_max >= 1 && zbins_max <= F64_MAX_COLS,
+                    "dfcsr_wake_fp64: zbins must be in [1, %d] (got %d)", F64_MAX_COLS, zbins_max);
     cudaStream_t st = as_stream(stream);
     const int64_t grid64 = n < (int64_t)(1 << 30) ? n : (int64_t)(1 << 30);
     ScopedTiming tm("wake_fp64", st);
     note_launch();
-    wake_fp64_kernel<<<(unsigned)grid64, F64_THREADS, 0, st>>>(jobs, job_of_point, s, x, n, dE, xkick);
+    if (zbins_max <= F64_STATIC_COLS) {
+        wake_fp64_kernel<false><<<(unsigned)grid64, F64_THREADS, 0, st>>>(
+            jobs, job_of_point, s, x, n, F64_STATIC_COLS, dE, xkick);
+    } else {
+        const size_t smem = (size_t)4 * zbins_max * sizeof(double);
+        int dev = 0;
+        DFCSR_CUDA_TRY(cudaGetDevice(&dev));
+        static std::mutex mu;
+        static size_t attr_set[64];
+        {
+            std::lock_guard<std::mutex> g(mu);
+            if (dev < 0 || dev >= 64) {
+                set_error("dfcsr_wake_fp64: device ordinal %d out of range", dev);
+                return DFCSR_BAD_ARG;
+            }
+            if (attr_set[dev] < smem) {
+                DFCSR_CUDA_TRY(cudaFuncSetAttribute(wake_fp64_kernel<true>,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)((size_t)4 * F64_MAX_COLS * sizeof(double))));
+                attr_set[dev] = (size_t)4 * F64_MAX_COLS * sizeof(double);
+            }
+        }
+        wake_fp64_kernel<true><<<(unsigned)grid64, F64_THREADS, smem, st>>>(
+            jobs, job_of_point, s, x, n, zbins_max, dE, xkick);
+    }
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }

@@ -341,7 +341,7 @@ class _BatchedWake:
                       self.ws.numel(), h)
         else:
             _lib.call("dfcsr_wake_fp64", ptr(self.jobs), ptr(self.jop), ptr(self.s), ptr(self.x), n,
-                      ptr(self.dE), ptr(self.xk), h)
+                      self.zbins, ptr(self.dE), ptr(self.xk), h)
 
     def _capture(self, k, stream):
         import torch

@@ -111,6 +111,9 @@ def test_bad_arguments_fail_without_gpu():
         _lib.call("dfcsr_deposit_cic2d_moments", ctypes.c_void_p(16), ctypes.c_void_p(16), None,
                   None, 10, 8, 8, ctypes.c_void_p(16), 0.0, 5.0, ctypes.c_void_p(16), None, None,
                   0, None)
+    with pytest.raises(_lib.DfcsrBadArgument, match="zbins"):
+        _lib.call("dfcsr_wake_fp64", ctypes.c_void_p(16), None, ctypes.c_void_p(16),
+                  ctypes.c_void_p(16), 5, 7000, ctypes.c_void_p(16), ctypes.c_void_p(16), None)
     # an empty wake is a no-op, with or without a job
     _lib.call("dfcsr_wake_mixed_job", None, None, None, 0, 100, 100, 0, None, None, None, 0, None)
     with pytest.raises(_lib.DfcsrBadArgument, match="extra_arrivals"):

@@ -274,6 +274,41 @@ def test_wake_fp64_bitwise_on_oracle_history():
     dE, xk = run.csr.wake_device(torch.from_numpy(s).cuda(), torch.from_numpy(x).cuda(), "fp64")
     np.testing.assert_array_equal(dE.cpu().numpy(), ref[0])
     np.testing.assert_array_equal(xk.cpu().numpy(), ref[1])
+    # more s' columns than the kernel's static shared memory holds (1024):
+    # the column sums go to dynamic shared memory, still bit for bit
+    zb = 1536
+    run.csr.integration_params.zbins = zb
+    w2 = O.WakeOracle(orc.tracker, orc.tables, orc.position, st["sigma_z"], st["sigma_x"],
+                      st["slope"][0], st["mean_x"], orc.lf, orc.integ["n_formation_length"], zb,
+                      orc.integ["xbins"], charge=orc.charge)
+    ref2 = w2.points(s[:2], x[:2])
+    dE2, xk2 = run.csr.wake_device(torch.from_numpy(s[:2]).cuda(), torch.from_numpy(x[:2]).cuda(),
+                                   "fp64")
+    np.testing.assert_array_equal(dE2.cpu().numpy(), ref2[0])
+    np.testing.assert_array_equal(xk2.cpu().numpy(), ref2[1])
+
+
+@cuda
+def test_wake_mixed_at_maximum_integration_bins():
+    """The mixed wake at its largest integration grid: 512 x' bins (the far
+    region's 1024 rows staged in shared memory) and 4096 s' bins (32 column
+    chunks per region), against the FP64 kernel with the same bins on three
+    observation points: max_rel, rms_rel and pointwise <= 1e-4."""
+    g = golden("wake_dipole.npz")
+    run = _device_run_from_fixture(g)
+    csr = run.csr
+    csr.get_CSR_mesh()
+    s, x = csr.mesh_device()
+    idx = torch.tensor([0, s.numel() // 2 + 7, s.numel() - 3], device="cuda")
+    s3, x3 = s[idx].contiguous(), x[idx].contiguous()
+    ip = csr.integration_params
+    ip.xbins, ip.zbins = 512, 4096
+    dE64, xk64 = csr.wake_device(s3, x3, "fp64")
+    dE, xk = csr.wake_device(s3, x3, "mixed")
+    ref = (dE64.cpu().numpy(), xk64.cpu().numpy())
+    assert np.isfinite(ref[0]).all() and np.isfinite(ref[1]).all()
+    e = wake_errors(dE.cpu().numpy(), xk.cpu().numpy(), *ref)
+    assert max(e.values()) <= 1e-4, e
 
 
 @cuda
