@@ -1,0 +1,65 @@
+"""The reference's run loop with the CSR kick applied every step
+(CSR.py:297-334: transport, DF and history, mesh, wake, Beam.apply_wakes),
+on the GPU with the plain FP64 wake against the oracle doing the same steps
+on the host.  The kick feeds back into every later step, so this pins the
+whole loop: transport, the moments-sized deposit, DF finalisation, history,
+mesh, wake and the kick interpolation.
+
+Tolerance: the FP64 wake is bit-exact with the oracle on the same history;
+the device DF/history sums are evaluated in fixed orders of their own
+(<= 1e-12 of the fields), so after the kicks of several steps every
+coordinate row agrees with the oracle's to 1e-9 of that row's largest
+kick-induced change (px, pz) or of its spread (the other rows)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from tests.helpers import OracleRun
+
+pytestmark = pytest.mark.gpu
+cuda = pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+
+
+@cuda
+def test_kick_loop_fp64_matches_oracle():
+    import bench
+    from pydfcsr_gb300.harness import WakeRun
+    from pydfcsr_gb300.synthetic import dipole_lattice, gaussian_beam
+    lat = dipole_lattice(1.5, 0.05, 0.01)
+    beam6 = gaussian_beam(60_000, 10e-6, 20e-6, 1e-4, 5e-6, -5.0, seed=21)
+    dep = {"xbins": 64, "zbins": 64, "xlim": 5, "zlim": 5, "filter_order": 2,
+           "filter_window": 5, "velocity_threhold": 1000}
+    integ = {"n_formation_length": 1.5, "zbins": 16, "xbins": 16}
+    mesh = {"xbins": 8, "zbins": 8, "xlim": 3, "zlim": 3}
+    step = float(lat["step_size"])
+    steps = 4
+    run = WakeRun(lat, beam6, dep, integ, mesh, precision="fp64", grid_rule="configured",
+                  host_transport=False)
+    bench.tracking_steps(run, 1, steps, "fp64", step)
+    torch.cuda.synchronize()
+    gpu = run.beam.particle.cpu().numpy()
+
+    orc = OracleRun(lat, beam6, dep, integ, grid_rule="configured")
+    orc.init()
+    for k in range(1, steps + 1):
+        orc.step(k)
+        st = orc.stats()
+        xm, zm, zr, xr = O.csr_mesh(st, mesh["xbins"], mesh["zbins"], mesh["xlim"], mesh["zlim"])
+        dE, xk = orc.wake_oracle().points(orc.position + zm, xm)
+        shape = (mesh["xbins"], mesh["zbins"])
+        orc.beam6 = O.apply_wakes(orc.beam6, dE.reshape(shape), xk.reshape(shape), xr, zr, step,
+                                  1e9, True, st["slope"])
+    # the beam without kicks, for the size of the kicks
+    free = beam6.copy()
+    for k in range(1, steps + 1):
+        free = run.plan.matrix(k) @ free
+    rel = []
+    for r in range(6):
+        kick = np.abs(orc.beam6[r] - free[r]).max()
+        scale = kick if r in (1, 5) else max(kick, np.abs(free[r]).max())
+        assert scale > 0, r
+        rel.append(float(np.abs(gpu[r] - orc.beam6[r]).max() / scale))
+    print("kick loop vs oracle, per row (of the row's scale):", ["%.1e" % v for v in rel])
+    assert max(rel) <= 1e-9, rel
+    assert np.abs(orc.beam6[5] - free[5]).max() > 0, "the kicks must change pz"
