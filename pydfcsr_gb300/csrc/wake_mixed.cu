@@ -63,7 +63,9 @@ constexpr int RW = 8;
 //  0: t cell (int), z cell (int), t offset (dw)        history coordinates at x'_ref
 //  1: z offset (dw), r0 = |R0| (dw)                    R0 = r(s) + x n(s) - r(s') - x'_ref n(s')
 //  2: u* = R0.n' / g (dw), rmin^2 = (R0 x n')^2 / g (dw)   foot of the perpendicular from
-//     the observer to the line x' -> r(s') + x' n(s'): |r - r'|^2 = rmin^2 + g (u - u*)^2
+//     the observer to the line x' -> r(s') + x' n(s'): |r - r'|^2 = rmin^2 + g (u - u*)^2;
+//     for s' outside the orbit tables (interpolate1D gives n' = tau' = 0, g = 0, as the
+//     reference's) u* = 0 and rmin^2 = r0^2, so that |r - r'| = r0 for every x
 //  3: g - 1, K0x = b - a e (dw), curvature at s'       g = |n'|^2
 //  4: a = v.tau', b = v.n', e = tau'.n', h = |tau'|^2
 //  5: K1x - 1 = a g - 1 + b e, K2x = b g, K0z = a (1 - h), K1z = a e + b h
@@ -218,7 +220,8 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
     const dw xref = gs.xrefw[r];
     const dw rx0 = dw_sub(dw_sub(gs.Px, L[0]), dw_mul(xref, npx));
     const dw ry0 = dw_sub(dw_sub(gs.Py, L[1]), dw_mul(xref, npy));
-    const dw r0 = dw_sqrt(dw_add_abs(dw_mul(rx0, rx0), dw_mul(ry0, ry0)));   // both >= 0
+    const dw r02 = dw_add_abs(dw_mul(rx0, rx0), dw_mul(ry0, ry0));   // both >= 0
+    const dw r0 = dw_sqrt(r02);
     const dw ut0 = dw_mul(dw_sub(gs.T0, r0), gs.inv_t);
     const dw uz0 = dw_mul(dw_add(dw_sub(spj, gs.Tz), r0), gs.inv_z);
     const float tfl = dw_floor(ut0), zfl = dw_floor(uz0);
@@ -248,8 +251,11 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
     const float ws = (j == 0 || j == gs.ax_s[r].n - 1) ? gs.wsf[r][0] : gs.wsf[r][1];
     const dw R0n = dw_add_abs(dw_mul(rx0, npx), dw_mul(ry0, npy));
     const dw cr = dw_sub_abs(dw_mul(rx0, npy), dw_mul(ry0, npx));
-    const dw us = dw_div(R0n, g);
-    const dw rmin2 = dw_div(dw_mul(cr, cr), g);
+    // s' outside the orbit tables: n' = 0 (g = 0), the distance is r0 for
+    // every x' (the integral's g (u - u*)^2 term vanishes with g - 1 = -1)
+    const bool no_normal = !(g.hi > 0.f);
+    const dw us = no_normal ? dw{0.f, 0.f} : dw_div(R0n, g);
+    const dw rmin2 = no_normal ? r02 : dw_div(dw_mul(cr, cr), g);
     const dw toff = dw_add_f(ut0, -tfl), zoff = dw_add_f(uz0, -zfl);
     const dw K0x = dw_sub(bb, ae);
     o[0] = make_float4(__int_as_float(cell_of(tfl, dw_isnan(ut0))),
@@ -366,7 +372,11 @@ __device__ __noinline__ void geometry_fp64(const dfcsr_wake_job &J, GeoShared &g
         float4 *o = reinterpret_cast<float4 *>(prec + gs.rm[r].col_off) + (size_t)j * (CW / 4);
         const double R0n = rx0 * npx + ry0 * npy, cr = rx0 * npy - ry0 * npx;
         const dw toff = dw_from(ut0 - tfl), zoff = dw_from(uz0 - zfl), r0w = dw_from(r0);
-        const dw us = dw_from(R0n / g), rmin2 = dw_from(cr * cr / g), K0x = dw_from(bb - a * e);
+        // s' outside the orbit tables: n' = 0, the distance is r0 for every x'
+        const bool no_normal = !(g > 0.0);
+        const dw us = no_normal ? dw{0.f, 0.f} : dw_from(R0n / g);
+        const dw rmin2 = no_normal ? dw_from(rx0 * rx0 + ry0 * ry0) : dw_from(cr * cr / g);
+        const dw K0x = dw_from(bb - a * e);
         o[0] = make_float4(__int_as_float(cell_index(ut0, tfl)), __int_as_float(cell_index(uz0, zfl)),
                            toff.hi, toff.lo);
         o[1] = make_float4(zoff.hi, zoff.lo, r0w.hi, r0w.lo);

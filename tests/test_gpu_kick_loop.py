@@ -3,7 +3,8 @@
 on the GPU with the plain FP64 wake against the oracle doing the same steps
 on the host.  The kick feeds back into every later step, so this pins the
 whole loop: transport, the moments-sized deposit, DF finalisation, history,
-mesh, wake and the kick interpolation.
+mesh, wake and the kick interpolation.  The same loop with the mixed wake
+applies kicks within 1e-4 of the FP64 loop's.
 
 Tolerance: the FP64 wake is bit-exact with the oracle on the same history;
 the device DF/history sums are evaluated in fixed orders of their own
@@ -39,6 +40,12 @@ def test_kick_loop_fp64_matches_oracle():
     bench.tracking_steps(run, 1, steps, "fp64", step)
     torch.cuda.synchronize()
     gpu = run.beam.particle.cpu().numpy()
+    # the same loop with the mixed wake
+    runm = WakeRun(lat, beam6, dep, integ, mesh, precision="mixed", grid_rule="configured",
+                   host_transport=False)
+    bench.tracking_steps(runm, 1, steps, "mixed", step)
+    torch.cuda.synchronize()
+    gpum = runm.beam.particle.cpu().numpy()
 
     orc = OracleRun(lat, beam6, dep, integ, grid_rule="configured")
     orc.init()
@@ -62,4 +69,45 @@ def test_kick_loop_fp64_matches_oracle():
         rel.append(float(np.abs(gpu[r] - orc.beam6[r]).max() / scale))
     print("kick loop vs oracle, per row (of the row's scale):", ["%.1e" % v for v in rel])
     assert max(rel) <= 1e-9, rel
+    # mixed wake in the loop: the kicks it applies (px, pz changes) within
+    # 1e-4 of the FP64 loop's, the other rows at their usual agreement
+    for r in (1, 5):
+        kick = np.abs(gpu[r] - free[r]).max()
+        d = np.abs((gpum[r] - free[r]) - (gpu[r] - free[r])).max()
+        print("mixed vs fp64 kick, row", r, "%.1e" % (d / kick))
+        assert d <= 1e-4 * kick, (r, d / kick)
     assert np.abs(orc.beam6[5] - free[5]).max() > 0, "the kicks must change pz"
+
+
+@cuda
+@pytest.mark.parametrize("bins", [(16, 16), (100, 100)])
+def test_wake_mixed_with_columns_before_the_orbit_start(bins):
+    """One step into a dipole (s = 0.01 m) the far region reaches s' < 0,
+    more than one orbit-table step before the lattice starts, where the
+    reference's interpolate1D gives n' = tau' = 0 (|r - r'| = |R0| for every
+    x').  The mixed wake (its distance from the perpendicular foot, which
+    divides by |n'|^2) must handle those columns: within 1e-4 of the FP64
+    wake, finite everywhere."""
+    from pydfcsr_gb300.harness import WakeRun
+    from pydfcsr_gb300.synthetic import dipole_lattice, gaussian_beam
+    from tests.helpers import wake_errors
+    lat = dipole_lattice(1.5, 0.05, 0.01)
+    beam6 = gaussian_beam(60_000, 10e-6, 20e-6, 1e-4, 5e-6, -5.0, seed=21)
+    dep = {"xbins": 64, "zbins": 64, "xlim": 5, "zlim": 5, "filter_order": 2,
+           "filter_window": 5, "velocity_threhold": 1000}
+    integ = {"n_formation_length": 1.5, "zbins": bins[1], "xbins": bins[0]}
+    mesh = {"xbins": 8, "zbins": 8, "xlim": 3, "zlim": 3}
+    run = WakeRun(lat, beam6, dep, integ, mesh, precision="both", grid_rule="configured",
+                  host_transport=False)
+    run.step(1)
+    csr = run.csr
+    csr.get_CSR_mesh()
+    s, x = csr.mesh_device()
+    sh = s.cpu().numpy()
+    regions = [csr._regions(v, 0.0)[1] for v in sh]
+    assert any(r[0][5] < -csr.lattice.delta_x for r in regions), "no column before the orbit start"
+    dE, xk = (t.cpu().numpy() for t in csr.wake_device(s, x, "mixed"))
+    d64, x64 = (t.cpu().numpy() for t in csr.wake_device(s, x, "fp64"))
+    assert np.isfinite(dE).all() and np.isfinite(xk).all()
+    e = wake_errors(dE, xk, d64, x64)
+    assert max(e.values()) <= 1e-4, e
