@@ -111,3 +111,15 @@ def test_wake_mixed_with_columns_before_the_orbit_start(bins):
     assert np.isfinite(dE).all() and np.isfinite(xk).all()
     e = wake_errors(dE, xk, d64, x64)
     assert max(e.values()) <= 1e-4, e
+    # the same with the mixed kernel's FP64 geometry (jobs without the
+    # double-word orbit tables)
+    from pydfcsr_gb300.CSR import jobs_to_device
+    job = csr._job()
+    job.lattice_dw = None
+    job.lattice_delta_dw = None
+    ip = csr.integration_params
+    g = csr.evaluator.mixed(jobs_to_device([job]), s, x, ip.xbins, ip.zbins)
+    dEg, xkg = g[0].cpu().numpy(), g[1].cpu().numpy()
+    assert np.isfinite(dEg).all() and np.isfinite(xkg).all()
+    e = wake_errors(dEg, xkg, d64, x64)
+    assert max(e.values()) <= 1e-4, e
