@@ -130,10 +130,11 @@ def test_large_beam_full_size_mixed_vs_fp64_with_band():
 def test_chicane_whole_run_mixed_vs_fp64():
     """The benchmark's chicane beam over all 100 steps (both branches of
     get_CSR_wake, the first steps with two or three history slices), every
-    5th step and the first two."""
+    5th step and the first two, without and with the FP64 near band
+    (20 sigma_z)."""
     steps = (1, 2) + tuple(range(5, 101, 5))
-    out = _mixed_vs_fp64("chicane_c2", 100, steps)
+    out = _mixed_vs_fp64("chicane_c2", 100, steps, near_band=20 * 50e-6)
     assert any(slope > 1.0 for _, slope, _ in out) and any(slope < 1.0 for _, slope, _ in out)
     for k, slope, res in out:
-        e = res[0.0]
-        assert max(e.values()) <= 1e-4, (k, slope, e)
+        for band, e in res.items():
+            assert max(e.values()) <= 1e-4, (k, slope, band, e)

@@ -123,3 +123,47 @@ def test_wake_mixed_with_columns_before_the_orbit_start(bins):
     assert np.isfinite(dEg).all() and np.isfinite(xkg).all()
     e = wake_errors(dEg, xkg, d64, x64)
     assert max(e.values()) <= 1e-4, e
+
+
+@cuda
+def test_wake_mixed_with_columns_past_the_orbit_end():
+    """At the last step of a lattice without a tail drift (s = 0.05 m, the
+    dipole's end) every near region reaches s' = s + 5 sigma_z beyond the
+    orbit tables' last sample, where interpolate1D (interp1D.py:14-36) gives
+    zero vectors, and the bunch's head half sits beyond it too.  Observers
+    with int((s - s_0) / ds) >= Nsample have zero orbit vectors of their own,
+    and the reference's wake there is NaN (dE and x_kick; the oracle gives
+    NaN at exactly those points).  Both device paths give NaN at the same
+    points; everywhere else the mixed wake is finite and within 1e-4 of the
+    FP64 wake."""
+    from pydfcsr_gb300.harness import WakeRun
+    from pydfcsr_gb300.synthetic import dipole_lattice, gaussian_beam
+    from tests.helpers import wake_errors
+    lat = dipole_lattice(1.5, 0.05, 0.01, tail_drift=0.0)
+    beam6 = gaussian_beam(60_000, 10e-6, 20e-6, 1e-4, 5e-6, -5.0, seed=22)
+    dep = {"xbins": 64, "zbins": 64, "xlim": 5, "zlim": 5, "filter_order": 2,
+           "filter_window": 5, "velocity_threhold": 1000}
+    integ = {"n_formation_length": 1.5, "zbins": 32, "xbins": 16}
+    mesh = {"xbins": 8, "zbins": 8, "xlim": 3, "zlim": 3}
+    run = WakeRun(lat, beam6, dep, integ, mesh, precision="both", grid_rule="configured",
+                  host_transport=False)
+    last = len(run.plan.positions) - 1
+    for k in range(1, last + 1):
+        run.step(k)
+    csr = run.csr
+    csr.get_CSR_mesh()
+    s, x = csr.mesh_device()
+    sh = s.cpu().numpy()
+    lt = csr.lattice
+    regions = [csr._regions(v, 0.0)[1] for v in sh]
+    assert all(r[-1][5] > lt.max_x + lt.delta_x for r in regions), "near regions must pass the end"
+    past = ((sh - lt.min_x) / lt.delta_x).astype(int) >= lt.s.shape[0]
+    assert past.any() and not past.all()
+    dE, xk = (t.cpu().numpy() for t in csr.wake_device(s, x, "mixed"))
+    d64, x64 = (t.cpu().numpy() for t in csr.wake_device(s, x, "fp64"))
+    for a in (dE, xk, d64, x64):
+        assert (np.isnan(a) == past).all()
+    inside = ~past
+    assert np.isfinite(dE[inside]).all() and np.isfinite(xk[inside]).all()
+    e = wake_errors(dE[inside], xk[inside], d64[inside], x64[inside])
+    assert max(e.values()) <= 1e-4, e
