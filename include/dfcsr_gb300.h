@@ -188,7 +188,8 @@ size_t dfcsr_df_workspace_bytes(int nx, int nz);
  * [nx-1], dzg [nz-1] (diff of each grid), equal to the host's numpy values
  * bit for bit.  x_uniform / z_uniform: whether numpy takes its
  * uniform-spacing branch (all differences equal; the caller decides it
- * from its host grid).  One launch on `stream`, device pointers out. */
+ * from its host grid).  2 <= nx, nz <= 2^24.  One launch on `stream`,
+ * device pointers out. */
 int dfcsr_df_axis_tables(double x0, double x1, int nx, double z0, double z1, int nz,
                          int x_uniform, int z_uniform, double *gx, double *gz,
                          double *dxg, double *dzg, void *stream);
@@ -234,7 +235,7 @@ int dfcsr_grid_barrier_check(int blocks, int extra_arrivals, unsigned int max_sp
  * append_interpolant's x_grid_interp / z_grid_interp, deposit.py:170-171,
  * 347-350): idx[ntgt], w[ntgt], oob[ntgt] computed on the device with the
  * RegularGridInterpolator rule above, equal to the host computation from the
- * numpy arrays. */
+ * numpy arrays.  2 <= nsrc <= 2^24, 1 <= ntgt <= 2^24. */
 int dfcsr_rgi_axis_linspace(double src_start, double src_stop, int nsrc,
                             double tgt_start, double tgt_stop, int ntgt, int32_t *idx,
                             double *w, uint8_t *oob, void *stream);

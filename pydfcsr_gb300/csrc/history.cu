@@ -183,11 +183,17 @@ __global__ void df_axis_tables(double x0, double x1, int nx, double z0, double z
 
 using namespace dfcsr;
 
+// Longest grid axis the table entry points accept (keeps their launch sizes
+// in int range; DF and history grids are a few thousand points at most).
+static constexpr int kMaxAxisPoints = 1 << 24;
+
 extern "C" int dfcsr_rgi_axis_linspace(double src_start, double src_stop, int nsrc,
                                        double tgt_start, double tgt_stop, int ntgt, int32_t *idx,
                                        double *w, uint8_t *oob, void *stream) {
     clear_error();
     DFCSR_CHECK_ARG(nsrc >= 2 && ntgt >= 1, "dfcsr_rgi_axis_linspace: need nsrc >= 2, ntgt >= 1");
+    DFCSR_CHECK_ARG(nsrc <= kMaxAxisPoints && ntgt <= kMaxAxisPoints,
+                    "dfcsr_rgi_axis_linspace: axes longer than %d points", kMaxAxisPoints);
     DFCSR_CHECK_ARG(idx && w && oob, "dfcsr_rgi_axis_linspace: null pointer");
     DFCSR_CHECK_ARG(src_stop > src_start, "dfcsr_rgi_axis_linspace: source grid must ascend");
     note_launch();
@@ -234,6 +240,8 @@ extern "C" int dfcsr_df_axis_tables(double x0, double x1, int nx, double z0, dou
                                     double *dxg, double *dzg, void *stream) {
     clear_error();
     DFCSR_CHECK_ARG(nx >= 2 && nz >= 2, "dfcsr_df_axis_tables: grids need >= 2 points (%d, %d)", nx, nz);
+    DFCSR_CHECK_ARG(nx <= kMaxAxisPoints && nz <= kMaxAxisPoints,
+                    "dfcsr_df_axis_tables: grids longer than %d points", kMaxAxisPoints);
     DFCSR_CHECK_ARG(gx && gz && dxg && dzg, "dfcsr_df_axis_tables: null pointer");
     note_launch();
     const int total = nx + nz;

@@ -104,6 +104,13 @@ def test_bad_arguments_fail_without_gpu():
     with pytest.raises(_lib.DfcsrBadArgument, match="grids need"):
         _lib.call("dfcsr_df_axis_tables", 0.0, 1.0, 1, 0.0, 1.0, 8, 0, 0, ctypes.c_void_p(16),
                   ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16), None)
+    with pytest.raises(_lib.DfcsrBadArgument, match="longer than"):
+        _lib.call("dfcsr_df_axis_tables", 0.0, 1.0, (1 << 24) + 1, 0.0, 1.0, 2**31 - 1, 0, 0,
+                  ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16),
+                  ctypes.c_void_p(16), None)
+    with pytest.raises(_lib.DfcsrBadArgument, match="longer than"):
+        _lib.call("dfcsr_rgi_axis_linspace", 0.0, 1.0, 8, 0.0, 1.0, 2**31 - 1,
+                  ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16), None)
     with pytest.raises(_lib.DfcsrBadArgument, match="moments is null"):
         _lib.call("dfcsr_deposit_cic2d_moments", ctypes.c_void_p(16), ctypes.c_void_p(16), None,
                   None, 10, 8, 8, None, 5.0, 5.0, ctypes.c_void_p(16), None, None, 0, None)
