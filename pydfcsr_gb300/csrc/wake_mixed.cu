@@ -1077,8 +1077,10 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
 // of the kernel's L2 traffic) 2.09; two 256-thread CTAs at 120 registers
 // 1.92; four 128-thread CTAs 1.76 (fewer warps wait at each unit-end
 // barrier and four work units per SM stage their records independently);
-// 96- or 64-thread CTAs 1.87 / 1.93.  128 registers leave no room for the
-// moments CTA, which then waits for the whole integral.  Defining
+// 96- or 64-thread CTAs 1.87 / 1.93; five 128-thread CTAs at 96 registers
+// (136 bytes of spills; the same 4096 registers left over) 1.79.  128
+// registers leave no room for the moments CTA, which then waits for the
+// whole integral.  Defining
 // MX_INTEGRAL_MAXREG as 0 selects __launch_bounds__ with
 // MX_INTEGRAL_BLOCKS CTAs per SM instead.
 #ifndef MX_INTEGRAL_MAXREG
