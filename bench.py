@@ -475,10 +475,13 @@ def build_history(run, upto):
         run.step(k)
 
 
-def time_workload(name, precision, W, K, side, first=None, n_particles=None, points_note=""):
+def time_workload(name, precision, W, K, side, first=None, n_particles=None, points_note="",
+                  peaks=None):
     """Time K steps of a workload (DF + history + wake on its whole mesh)
     after W warm-up steps, pipelined like the headline loop.  Returns the
-    measurement and the run (its last step's wake in run.last)."""
+    measurement and the run (its last step's wake in run.last).  With
+    ``peaks`` = (HBM GB/s, FMA peaks, SM clock MHz) the measurement also
+    carries each stage's roofline and the dominant kernel's."""
     import torch
     from pydfcsr_gb300 import _lib
     from pydfcsr_gb300.synthetic import workload
@@ -510,6 +513,16 @@ def time_workload(name, precision, W, K, side, first=None, n_particles=None, poi
            "warmup": W, "ms_per_step": ms, "wake_points_per_s": npts * 1000.0 / ms,
            "mesh_points": npts, "step_ms_p50": float(np.median([a.elapsed_time(b) for a, b in ev])),
            "kernel_ms_per_step": {n: round(v[0] / K, 4) for n, v in kt.items() if v[1]}}
+    if peaks is not None:
+        hbm, fma_peaks, clock_mhz = peaks
+        kname = "wake_mixed_integral" if precision == "mixed" else "wake_fp64"
+        k_ms, k_n = kt[kname]
+        if k_n:
+            n_sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+            out["roofline"] = roofline(kname, k_ms / k_n, k_n,
+                                       integrand_points(wl, run, range(first, first + K)), npts,
+                                       fma_peaks, hbm, precision, clock_mhz, n_sms)
+        out["stages"] = stage_rooflines(kt, K, wl, run, hbm, fma_peaks)
     return out, run, wl
 
 
@@ -725,7 +738,8 @@ def gpu_arm(a):
         out["timed_window_branches"] = {"steps": [first, last],
                                         "3_region": sum(r["regions"] == 3 for r in rows),
                                         "4_region": sum(r["regions"] == 4 for r in rows)}
-        out["workloads"] = other_workloads(W, K, side, out["accuracy"])
+        out["workloads"] = other_workloads(W, K, side, out["accuracy"],
+                                           peaks=(hbm, fma_peaks, ck.get("sm_mhz")))
 
     if a.serve_requests > 0 and a.precision == "mixed":
         out["serving"] = serving_leg(a.serve_requests, a.serve_rate, a.serve_fp64_every,
@@ -775,7 +789,7 @@ def full_run(wl, precision, side):
                           "have short histories)"}
 
 
-def other_workloads(W, K, side, accuracy):
+def other_workloads(W, K, side, accuracy, peaks=None):
     """C1 (the plain FP64 drop-in on the dipole, at its exit), C3 (double-horn
     chicane) and C5 (large beam, 300 steps): a timed window each, and the
     accuracy scans of C3 and C5."""
@@ -786,7 +800,8 @@ def other_workloads(W, K, side, accuracy):
     # up to the dipole exit (step 300), and the mixed form on the same steps
     c1 = {}
     for prec in ("fp64", "mixed"):
-        m, run, wl = time_workload("dipole_c1", prec, min(W, 3), K1, side, first=300 - K1 + 1)
+        m, run, wl = time_workload("dipole_c1", prec, min(W, 3), K1, side, first=300 - K1 + 1,
+                                   peaks=peaks)
         c1[prec] = m
         dE, xk = (t.cpu().numpy() for t in run.last)
         c1[prec + "_last"] = (dE, xk)
@@ -797,7 +812,7 @@ def other_workloads(W, K, side, accuracy):
     c1["mixed_speedup"] = c1["fp64"]["ms_per_step"] / c1["mixed"]["ms_per_step"]
     out["C1_dipole"] = c1
     for key, name, every in (("C3_double_horn", "chicane_c3", 4), ("C5_large_beam", "chicane_c5", 10)):
-        m, run, wl = time_workload(name, "mixed", W, K, side)
+        m, run, wl = time_workload(name, "mixed", W, K, side, peaks=peaks)
         del run
         torch.cuda.empty_cache()
         m64, run, _ = time_workload(name, "fp64", 2, 2, side, first=m["steps"][1] - 1)
@@ -907,7 +922,7 @@ def stage_rooflines(kt, K, wl, run, hbm, fma_peaks):
                           "FP64 pipe (moment sums) and the latency of the sort passes"),
         "df_finalize": (7 * 8.0 * cells, None, "2 fields read + 5 written, 8 B per cell",
                         "latency of nine dependent phases (grid barriers, FP64 reductions) over "
-                        "a grid of ~65k cells"),
+                        f"a grid of {cells} cells"),
         "history_regrid": (32.0 * nxi * nzi + 40.0 * cells, 40.0 * nxi * nzi,
                            "one FP32 ring slot written (32 B per cell) + 5 source fields read; "
                            "5 fields x 4 corners x 2 FP64 operations per target cell",
