@@ -49,6 +49,26 @@ long long dfcsr_kernel_launches(void);
  * bindings that lay the structs out themselves); 0 for other values. */
 size_t dfcsr_abi_sizeof(int which);
 
+/* Bounds-checked build (no reference counterpart; stands in for
+ * compute-sanitizer).  libdfcsr_gb300_checked.so is this library built with
+ * -DDFCSR_BOUNDS_CHECK=1: every kernel tests its computed global-memory
+ * indices (history cells, per-point records, sort positions, particle
+ * indices, table cells) against their buffers; the first failing test
+ * records bit 63 | site << 48 | (index & 0xffffffffffff) in a device
+ * status word and the access is skipped (nothing traps).  Sites: 1 probe,
+ * 10-13 mixed integral / set-up, 20 mixed geometry, 30 FP64 history
+ * gathers, 31 orbit tables, 40-43
+ * deposit, 50 history regrid, 60 apply_wakes, 70 DF stage, 80 interp3d /
+ * interp1d.  dfcsr_bounds_checked: 1 in the checked library, 0 otherwise.
+ * dfcsr_bounds_status: synchronises the device and gives the first failure
+ * (0: none), clearing the status words when `reset`; in the release library
+ * it gives 0 without touching the device.  dfcsr_bounds_probe: one thread
+ * tests `index` against [0, size) at `site` (1..32767) through the same
+ * check, without accessing memory (a test of the mechanism itself). */
+int dfcsr_bounds_checked(void);
+int dfcsr_bounds_status(unsigned long long *first_failure, int reset);
+int dfcsr_bounds_probe(long long index, long long size, int site, void *stream);
+
 /* Optional kernel timing (off by default).  When enabled, the entry points
  * record CUDA events around their main kernels on the launch stream;
  * dfcsr_timing_collect() waits for the recorded events and adds their

@@ -102,6 +102,9 @@ _SIGS = [
     ("dfcsr_last_error", ctypes.c_char_p, []),
     ("dfcsr_status_name", ctypes.c_char_p, [_c_int]),
     ("dfcsr_abi_sizeof", _c_size, [_c_int]),
+    ("dfcsr_bounds_checked", _c_int, []),
+    ("dfcsr_bounds_status", _c_int, [ctypes.POINTER(ctypes.c_ulonglong), _c_int]),
+    ("dfcsr_bounds_probe", _c_int, [ctypes.c_longlong, ctypes.c_longlong, _c_int, _p]),
     ("dfcsr_timing_enable", None, [_c_int]),
     ("dfcsr_timing_collect", _c_int, []),
     ("dfcsr_timing_get", _c_int, [ctypes.c_char_p, ctypes.POINTER(_c_double),
@@ -153,19 +156,28 @@ _lib = None
 _lock = threading.Lock()
 
 
+def checked_requested():
+    """Whether this process loads the bounds-checked library
+    (DFCSR_GB300_CHECKED=1 in the environment)."""
+    return os.environ.get("DFCSR_GB300_CHECKED", "") == "1"
+
+
 def library_path():
-    return _build.LIB
+    return _build.lib_path(checked_requested())
 
 
 def load(build_if_needed=True):
-    """Load (building first if the sources are newer) and return the CDLL."""
+    """Load (building first if the sources are newer) and return the CDLL:
+    the release library, or the bounds-checked one when
+    DFCSR_GB300_CHECKED=1."""
     global _lib
     with _lock:
         if _lib is not None:
             return _lib
-        path = _build.LIB
-        if build_if_needed and not _build.up_to_date():
-            _build.build()
+        checked = checked_requested()
+        path = _build.lib_path(checked)
+        if build_if_needed and not _build.up_to_date(checked):
+            _build.build(checked=checked)
         if not os.path.exists(path):
             raise ImportError(f"dfcsr_gb300 native library not found at {path}; run "
                               "`python -m pydfcsr_gb300.build` (needs nvcc for sm_103a)")
@@ -195,6 +207,20 @@ def call(name, *args):
 def query(name, *args):
     """Call a size / info function (no status)."""
     return getattr(load(), name)(*args)
+
+
+def bounds_status(reset=False):
+    """First index-check failure recorded by the bounds-checked library, as
+    (site, index), or None (always None in the release library).  Waits for
+    the device in the checked library."""
+    v = ctypes.c_ulonglong(0)
+    call("dfcsr_bounds_status", ctypes.byref(v), 1 if reset else 0)
+    if not v.value:
+        return None
+    idx = v.value & 0xFFFFFFFFFFFF
+    if idx >= 1 << 47:
+        idx -= 1 << 48
+    return (v.value >> 48) & 0x7FFF, idx
 
 
 def kernel_launches():

@@ -8,6 +8,12 @@ Each CUDA translation unit is compiled in parallel for
 library with a plain C ABI (``include/dfcsr_gb300.h``).  ``wake_fp64.cu`` is
 compiled with ``-fmad=false`` so that the FP64 drop-in kernel rounds every
 product and sum separately, like numpy.
+
+``build(checked=True)`` (``--checked``) builds the same sources with
+``-DDFCSR_BOUNDS_CHECK=1`` into ``libdfcsr_gb300_checked.so``: every kernel
+tests its computed global-memory indices, records the first failure in a
+status word read by ``dfcsr_bounds_status`` and skips the access.  Setting
+``DFCSR_GB300_CHECKED=1`` makes the Python package load that library.
 """
 import argparse
 import concurrent.futures as cf
@@ -20,6 +26,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libdfcsr_gb300.so")
+LIB_CHECKED = os.path.join(BUILD, "libdfcsr_gb300_checked.so")
+CHECKED_FLAGS = ["-DDFCSR_BOUNDS_CHECK=1"]
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -53,13 +61,18 @@ def _sources_mtime():
     return max(os.path.getmtime(f) for f in files)
 
 
-def up_to_date():
-    return os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime()
+def lib_path(checked=False):
+    return LIB_CHECKED if checked else LIB
 
 
-def _compile(unit, extra):
+def up_to_date(checked=False):
+    lib = lib_path(checked)
+    return os.path.exists(lib) and os.path.getmtime(lib) >= _sources_mtime()
+
+
+def _compile(unit, extra, objdir):
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
+    obj = os.path.join(objdir, unit.replace(".cu", ".o"))
     cmd = [nvcc()] + ARCH + COMMON + extra + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -67,27 +80,40 @@ def _compile(unit, extra):
     return obj
 
 
-def build(force=False, verbose=False):
-    """Compile (if needed) and return the path of the shared library."""
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose=False, checked=False):
+    """Compile (if needed) and return the path of the shared library (the
+    bounds-checked variant with ``checked``)."""
+    lib = lib_path(checked)
+    if not force and up_to_date(checked):
+        return lib
+    objdir = os.path.join(BUILD, "checked") if checked else BUILD
+    os.makedirs(objdir, exist_ok=True)
+    flags = CHECKED_FLAGS if checked else []
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        objs = list(ex.map(lambda kv: _compile(*kv), UNITS.items()))
-    tmp = LIB + f".{os.getpid()}.tmp"
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1] + flags, objdir), UNITS.items()))
+    tmp = lib + f".{os.getpid()}.tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
-        print(f"built {LIB}")
-    return LIB
+        print(f"built {lib}")
+    return lib
+
+
+def build_all(force=False, verbose=False):
+    """Both libraries, the release one and the bounds-checked one, compiled
+    side by side."""
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        futs = [ex.submit(build, force, verbose, c) for c in (False, True)]
+        return [f.result() for f in futs]
 
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")
+    ap.add_argument("--checked", action="store_true", help="the bounds-checked library")
     a = ap.parse_args()
-    print(build(force=a.force, verbose=True))
+    print(build(force=a.force, verbose=True, checked=a.checked))
     sys.exit(0)

@@ -142,7 +142,7 @@ apply_kicks(double *__restrict__ p, int64_t n, int64_t ld, const double *__restr
     double y0, y1;
     const bool in_x = rgi_lookup(gx, axes, nx, xt, i, y0);
     const bool in_z = rgi_lookup(gz, axes + (nx - 1), nz, z, j, y1);
-    const bool in = in_x && in_z;
+    const bool in = in_x && in_z && bounds_ok(i, nx - 1, BS_KICK) && bounds_ok(j, nz - 1, BS_KICK);
     const double u0 = __dsub_rn(1.0, y0), u1 = __dsub_rn(1.0, y1);
     const double dpz = in ? rgi_value(tables, nz, i, j, u0, u1, y0, y1) : 0.0;
     p[5 * ld + idx] = __dadd_rn(p[5 * ld + idx], dpz);
@@ -220,3 +220,5 @@ extern "C" int dfcsr_apply_wakes(double *coords, int64_t n, int64_t ld, const do
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }
+
+DFCSR_BOUNDS_READER(beam_ops)

@@ -63,6 +63,30 @@ extern "C" size_t dfcsr_abi_sizeof(int which) {
     }
 }
 
+// --------------------------------------------------------- bounds checks
+extern "C" int dfcsr_bounds_checked(void) { return DFCSR_BOUNDS_CHECK ? 1 : 0; }
+
+extern "C" int dfcsr_bounds_status(unsigned long long *first_failure, int reset) {
+    dfcsr::clear_error();
+    DFCSR_CHECK_ARG(first_failure, "dfcsr_bounds_status: null pointer");
+    *first_failure = 0;
+#if DFCSR_BOUNDS_CHECK
+    DFCSR_CUDA_TRY(cudaDeviceSynchronize());
+    cudaError_t (*const readers[])(unsigned long long *, bool) = {
+        dfcsr::bounds_read_beam_ops, dfcsr::bounds_read_deposit, dfcsr::bounds_read_dfstage,
+        dfcsr::bounds_read_history,  dfcsr::bounds_read_interp,  dfcsr::bounds_read_probe,
+        dfcsr::bounds_read_wake_fp64, dfcsr::bounds_read_wake_mixed};
+    for (auto rd : readers) {
+        unsigned long long v = 0;
+        DFCSR_CUDA_TRY(rd(&v, reset != 0));
+        if (*first_failure == 0) *first_failure = v;
+    }
+#else
+    (void)reset;   // the release library has no status words
+#endif
+    return DFCSR_OK;
+}
+
 // --------------------------------------------------------------- timing
 // Optional per-kernel timing: when enabled, entry points bracket their main
 // kernels with CUDA events recorded on the launch stream.  Events are read

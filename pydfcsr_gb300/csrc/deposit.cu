@@ -330,17 +330,19 @@ radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ va
         const uint32_t key = sm.u.t.key[i];
         const int d = (int)((key >> shift) & RS_MASK);
         const uint32_t pos = sm.dbase[d] + (uint32_t)i - sm.toff[d];
+        if (!bounds_ok(pos, n, BS_DEP_SCATTER)) continue;
         keys_out[pos] = key;
         vals_out[pos] = sm.u.t.val[i];
     }
 }
 
 // ------------------------------------------------------------- cell sums
-__global__ void cell_ranges(const uint32_t *__restrict__ keys, int64_t n,
+__global__ void cell_ranges(const uint32_t *__restrict__ keys, int64_t n, uint32_t nkeys,
                             uint32_t *__restrict__ cstart, uint32_t *__restrict__ cend) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t k = keys[i];
+    if (!bounds_ok(k, (long long)nkeys + 1, BS_DEP_CELL)) return;   // nkeys: outside the grid
     if (i == 0 || keys[i - 1] != k) cstart[k] = (uint32_t)i;
     if (i == n - 1 || keys[i + 1] != k) cend[k] = (uint32_t)(i + 1);
 }
@@ -453,7 +455,7 @@ seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, i
 #pragma unroll 1
     for (int j = 0; j < SEG_K; ++j) {
         const bool live = j < m && k < nkeys;      // outside-grid particles sort last
-        if (live)
+        if (live && bounds_ok(sv[seg_slot(off + j)], n, BS_DEP_PARTICLE))
             cell_accumulate<W0, W1>(sv[seg_slot(off + j)], fi1, fi2, q1, q2, w0, w1, inv1, inv2,
                                     acc);
         const uint32_t kn = (j + 1 < m) ? sk[seg_slot(off + j + 1)] : 0xffffffffu;
@@ -461,6 +463,7 @@ seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, i
             if (!W0) acc[0] = (double)(j + 1 - j0);
             const int64_t cs = cstart[k], ce = cend[k];
             if (cs >= b && ce <= e) store8(partial + (size_t)k * 8, acc);
+            else if (!bounds_ok(t, (n + SEG_K - 1) / SEG_K, BS_DEP_CHUNK)) {}
             else if (j0 == 0) store8(chunk_first + (size_t)t * 8, acc);
             else store8(chunk_last + (size_t)t * 8, acc);
 #pragma unroll
@@ -476,7 +479,7 @@ seg_sums(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, i
 }
 
 __global__ void seg_combine(const uint32_t *__restrict__ cstart, const uint32_t *__restrict__ cend,
-                            uint32_t nkeys, const double *__restrict__ chunk_first,
+                            uint32_t nkeys, int64_t nchunks, const double *__restrict__ chunk_first,
                             const double *__restrict__ chunk_last, double *__restrict__ partial) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nkeys) return;
@@ -488,6 +491,7 @@ __global__ void seg_combine(const uint32_t *__restrict__ cstart, const uint32_t 
     }
     const uint32_t t0 = cs / SEG_K, t1 = (ce - 1) / SEG_K;
     if (t0 == t1) return;                           // summed whole by seg_sums
+    if (!bounds_ok(t1, nchunks, BS_DEP_CHUNK)) return;
     const double *first = (cs == t0 * SEG_K) ? chunk_first : chunk_last;
 #pragma unroll
     for (int c = 0; c < 8; ++c) acc[c] = first[(size_t)t0 * 8 + c];
@@ -721,7 +725,7 @@ static int deposit_run(const char *fn, const double *q1, const double *q2, const
             t = vin; vin = vout; vout = t;
         }
         note_launch();
-        cell_ranges<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(kin, n, cs, ce);
+        cell_ranges<<<(unsigned)((n + tb - 1) / tb), tb, 0, s>>>(kin, n, L.nkeys, cs, ce);
         double *cfirst = reinterpret_cast<double *>(kout);
         double *clast = reinterpret_cast<double *>(vout);
         const unsigned sb = (unsigned)((n + SEG_TILE - 1) / SEG_TILE);
@@ -735,8 +739,8 @@ static int deposit_run(const char *fn, const double *q1, const double *q2, const
         else DFCSR_SEG(false, false);
 #undef DFCSR_SEG
         note_launch();
-        seg_combine<<<(unsigned)((L.nkeys + 255) / 256), 256, 0, s>>>(cs, ce, L.nkeys, cfirst,
-                                                                       clast, part);
+        seg_combine<<<(unsigned)((L.nkeys + 255) / 256), 256, 0, s>>>(
+            cs, ce, L.nkeys, (n + SEG_K - 1) / SEG_K, cfirst, clast, part);
     } else {
         DFCSR_CUDA_TRY(cudaMemsetAsync(part, 0, sizeof(double) * (size_t)L.nkeys * 8, s));
     }
@@ -778,3 +782,5 @@ extern "C" int dfcsr_deposit_cic2d_moments(const double *q1, const double *q2, c
     return deposit_run("dfcsr_deposit_cic2d_moments", q1, q2, w0, w1, n, nb1, nb2, DepGrid{}, moments,
                        lim1, lim2, out0, out1, workspace, workspace_bytes, as_stream(stream));
 }
+
+DFCSR_BOUNDS_READER(deposit)

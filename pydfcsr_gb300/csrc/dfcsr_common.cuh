@@ -75,6 +75,90 @@ struct ScopedTiming {
     ~ScopedTiming() { timing_end(tok, s); }
 };
 
+// ------------------------------------------------- bounds-checked build
+// Built with -DDFCSR_BOUNDS_CHECK=1 (libdfcsr_gb300_checked.so), the
+// kernels test each computed global-memory index (history cells, records,
+// sort positions, particle indices, table cells) against the extent of its
+// buffer before the access.  A failing test records
+//   bit 63 | site << 48 | (index & 0xffffffffffff)
+// in the translation unit's status word (the first failure wins), and the
+// access is skipped: nothing traps, the context stays usable, and
+// dfcsr_bounds_status reports the site and index.  In the release library
+// bounds_ok is the constant true and the tests compile away.
+enum BoundsSite : unsigned {
+    BS_PROBE = 1,             // dfcsr_bounds_probe
+    BS_MIXED_RING = 10,       // mixed integral: history cell (slot, x, z)
+    BS_MIXED_REC = 11,        // mixed integral: column / row records of a point
+    BS_MIXED_ROWS = 12,       // mixed integral: valid row range of a region
+    BS_MIXED_SETUP = 13,      // mixed set-up / band: history cells (FP64 gathers)
+    BS_GEO_REC = 20,          // mixed geometry: record writes
+    BS_FP64_RING = 30,        // FP64 wake and FP64 gathers: history cells
+    BS_ORBIT = 31,            // orbit-table sample (interpolate1D of the lattice tables)
+    BS_DEP_SCATTER = 40,      // deposit: radix scatter position
+    BS_DEP_PARTICLE = 41,     // deposit: particle index of a sorted entry
+    BS_DEP_CELL = 42,         // deposit: cell key
+    BS_DEP_CHUNK = 43,        // deposit: chunk part slot
+    BS_REGRID = 50,           // history regrid: source cell
+    BS_KICK = 60,             // apply_wakes: kick table cell
+    BS_DF = 70,               // DF stage: grid cell
+    BS_INTERP = 80,           // interpolate3D / interpolate1D: table cell
+};
+
+#ifndef DFCSR_BOUNDS_CHECK
+#define DFCSR_BOUNDS_CHECK 0
+#endif
+
+#if DFCSR_BOUNDS_CHECK
+static __device__ unsigned long long g_bounds_fail;   // one per translation unit
+
+static __device__ __noinline__ void bounds_record(long long i, unsigned site) {
+    const unsigned long long code = (1ull << 63) | ((unsigned long long)(site & 0x7fffu) << 48) |
+                                    ((unsigned long long)i & 0xffffffffffffull);
+    atomicCAS(&g_bounds_fail, 0ull, code);
+}
+
+__device__ __forceinline__ bool bounds_ok(long long i, long long n, unsigned site) {
+    if (i >= 0 && i < n) return true;
+    bounds_record(i, site);
+    return false;
+}
+#else
+__device__ __forceinline__ constexpr bool bounds_ok(long long, long long, unsigned) { return true; }
+#endif
+
+// Host: this translation unit's status word (0: no failure), cleared when
+// `reset`.  Each unit with kernels defines its reader with
+// DFCSR_BOUNDS_READER(name); capi.cu's dfcsr_bounds_status reads them all.
+#if DFCSR_BOUNDS_CHECK
+#define DFCSR_BOUNDS_READER(name)                                                          \
+    namespace dfcsr {                                                                      \
+    cudaError_t bounds_read_##name(unsigned long long *v, bool reset) {                    \
+        cudaError_t e = cudaMemcpyFromSymbol(v, g_bounds_fail, sizeof(*v));                \
+        if (e == cudaSuccess && reset) {                                                   \
+            const unsigned long long z = 0;                                                \
+            e = cudaMemcpyToSymbol(g_bounds_fail, &z, sizeof(z));                          \
+        }                                                                                  \
+        return e;                                                                          \
+    }                                                                                      \
+    }
+#else
+#define DFCSR_BOUNDS_READER(name)                                                          \
+    namespace dfcsr {                                                                      \
+    cudaError_t bounds_read_##name(unsigned long long *v, bool) {                          \
+        *v = 0;                                                                            \
+        return cudaSuccess;                                                                \
+    }                                                                                      \
+    }
+#endif
+cudaError_t bounds_read_beam_ops(unsigned long long *v, bool reset);
+cudaError_t bounds_read_deposit(unsigned long long *v, bool reset);
+cudaError_t bounds_read_dfstage(unsigned long long *v, bool reset);
+cudaError_t bounds_read_history(unsigned long long *v, bool reset);
+cudaError_t bounds_read_interp(unsigned long long *v, bool reset);
+cudaError_t bounds_read_probe(unsigned long long *v, bool reset);
+cudaError_t bounds_read_wake_fp64(unsigned long long *v, bool reset);
+cudaError_t bounds_read_wake_mixed(unsigned long long *v, bool reset);
+
 // ------------------------------------------------------------ device math
 // Reference axis rule of interpolate3D / interpolate1D: i0 = int(u)
 // (truncation toward zero), i1 = i0 unless i0 is the last index, in range iff

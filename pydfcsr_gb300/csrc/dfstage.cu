@@ -195,7 +195,9 @@ __device__ void sg_phase(const Load &load, double *const *dst, int nf, int nx, i
             int r, c;
             if (AXIS == 0) { r = idx / SG_TILE; c = idx % SG_TILE; }
             else { c = idx / rows; r = idx % rows; }
-            tile[r * ld + c] = (c < ncol) ? load(bf, lo + r, c0 + c) : 0.0;
+            tile[r * ld + c] = (c < ncol && bounds_ok(lo + r, L, BS_DF) && bounds_ok(c0 + c, M, BS_DF))
+                                   ? load(bf, lo + r, c0 + c)
+                                   : 0.0;
         }
         __syncthreads();
         for (int idx = threadIdx.x; idx < SG_TILE * SG_TILE; idx += blockDim.x) {
@@ -207,16 +209,19 @@ __device__ void sg_phase(const Load &load, double *const *dst, int nf, int nx, i
             // the window's weights (interior, left edge or right edge map) and
             // its first sample; two fused multiply-add chains (even / odd taps)
             const double *x, *e;
+            int r0;   // the window's first staged row
             if (l >= m && l < L - m) {
-                x = tile + (l - m - lo) * ld + c;
+                r0 = l - m - lo;
                 e = coef;
             } else if (l < m) {
-                x = tile + (0 - lo) * ld + c;
+                r0 = 0 - lo;
                 e = elo + (size_t)l * w;
             } else {
-                x = tile + (L - w - lo) * ld + c;
+                r0 = L - w - lo;
                 e = ehi + (size_t)(l - (L - m)) * w;
             }
+            if (!(bounds_ok(r0, rows, BS_DF) && bounds_ok(r0 + w - 1, rows, BS_DF))) continue;
+            x = tile + r0 * ld + c;
             double a0 = __dmul_rn(x[0], e[0]), a1 = 0.0;
             int k = 1;
             for (; k + 1 < w; k += 2) {
@@ -607,3 +612,4 @@ extern "C" int dfcsr_grid_barrier_check(int blocks, int extra_arrivals, unsigned
     return DFCSR_OK;
 }
 
+DFCSR_BOUNDS_READER(dfstage)

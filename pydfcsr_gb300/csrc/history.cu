@@ -22,7 +22,7 @@ namespace dfcsr {
 template <bool EXACT>
 __global__ void regrid5(const double *__restrict__ f0, const double *__restrict__ f1,
                         const double *__restrict__ f2, const double *__restrict__ f3,
-                        const double *__restrict__ f4, int snz,
+                        const double *__restrict__ f4, int snx, int snz,
                         const int32_t *__restrict__ ix, const double *__restrict__ wx,
                         const uint8_t *__restrict__ oobx, int nxi,
                         const int32_t *__restrict__ iz, const double *__restrict__ wz,
@@ -38,6 +38,7 @@ __global__ void regrid5(const double *__restrict__ f0, const double *__restrict_
         v[4] = *fill4;
     } else {
         const int i = ix[a], j = iz[c];
+        if (!(bounds_ok(i, snx - 1, BS_REGRID) && bounds_ok(j, snz - 1, BS_REGRID))) return;
         const double y0 = wx[a], y1 = wz[c];
         const double u0 = 1.0 - y0, u1 = 1.0 - y1;
         const size_t k00 = (size_t)i * snz + j, k01 = k00 + 1, k10 = k00 + snz, k11 = k10 + 1;
@@ -225,11 +226,11 @@ extern "C" int dfcsr_history_regrid(const double *density, const double *density
     note_launch();
     if (ring64_slot)
         regrid5<true><<<blocks, 256, 0, as_stream(stream)>>>(
-            density, density_x, density_z, vx, vx_x, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,
+            density, density_x, density_z, vx, vx_x, snx, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,
             vx_x_fill, ring64_slot, ring32_slot);
     else
         regrid5<false><<<blocks, 256, 0, as_stream(stream)>>>(
-            density, density_x, density_z, vx, vx_x, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,
+            density, density_x, density_z, vx, vx_x, snx, snz, ix, wx, oobx, nxi, iz, wz, oobz, nzi,
             vx_x_fill, ring64_slot, ring32_slot);
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
@@ -250,3 +251,5 @@ extern "C" int dfcsr_df_axis_tables(double x0, double x1, int nx, double z0, dou
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }
+
+DFCSR_BOUNDS_READER(history)

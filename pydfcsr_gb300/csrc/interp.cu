@@ -21,6 +21,11 @@ __global__ void interp3d_kernel(const double *__restrict__ qt, const double *__r
         out[i] = 0.0;
         return;
     }
+    if (!(bounds_ok(t1, nt, BS_INTERP) && bounds_ok(x1, nx, BS_INTERP) && bounds_ok(z1, nz, BS_INTERP) &&
+          bounds_ok(t0, nt, BS_INTERP) && bounds_ok(x0, nx, BS_INTERP) && bounds_ok(z0, nz, BS_INTERP))) {
+        out[i] = 0.0;
+        return;
+    }
     auto D = [&](int a, int b, int c) { return d[((size_t)a * nx + b) * nz + c]; };
     auto L = [](double p, double q, double w) {
         return __dadd_rn(__dmul_rn(p, __dsub_rn(1.0, w)), __dmul_rn(q, w));
@@ -41,6 +46,10 @@ __global__ void interp1d_kernel(const double *__restrict__ q, int64_t m, const d
     int a, b;
     double f;
     if (!axis_index(__ddiv_rn(__dsub_rn(q[i], min_x), delta_x), n, a, b, f)) {
+        out[i] = 0.0;
+        return;
+    }
+    if (!(bounds_ok(a, n, BS_INTERP) && bounds_ok(b, n, BS_INTERP))) {
         out[i] = 0.0;
         return;
     }
@@ -110,3 +119,5 @@ extern "C" int dfcsr_interp1d(const double *q, int64_t m, const double *table, i
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }
+
+DFCSR_BOUNDS_READER(interp)

@@ -1,6 +1,7 @@
 // Arithmetic-rate probe: the FP32 and FP64 fused multiply-add throughput of
 // this GPU, measured by the benchmark next to its results (the roofline
-// denominators for the FP32-bound and FP64-bound kernels of the wake path).
+// denominators for the FP32-bound and FP64-bound kernels of the wake path);
+// and the probe of the bounds-checked build's index check.
 #include "dfcsr_common.cuh"
 
 namespace dfcsr {
@@ -33,6 +34,21 @@ fma_probe(int64_t iters, T m, T c, T *sink) {
 
 using namespace dfcsr;
 
+// One thread tests `index` against [0, size) with the bounds-checked
+// build's check (no memory is accessed at that index).
+__global__ void bounds_probe(long long index, long long size, unsigned site) {
+    if (!dfcsr::bounds_ok(index, size, site)) return;
+}
+
+extern "C" int dfcsr_bounds_probe(long long index, long long size, int site, void *stream) {
+    clear_error();
+    DFCSR_CHECK_ARG(site > 0 && site < 0x8000, "dfcsr_bounds_probe: site %d outside 1..32767", site);
+    note_launch();
+    bounds_probe<<<1, 1, 0, as_stream(stream)>>>(index, size, (unsigned)site);
+    DFCSR_LAUNCH_CHECK();
+    return DFCSR_OK;
+}
+
 extern "C" int dfcsr_probe_fma(int fp64, int64_t iters, void *sink, double *flops, void *stream) {
     clear_error();
     DFCSR_CHECK_ARG(iters > 0 && sink && flops, "dfcsr_probe_fma: bad argument");
@@ -49,3 +65,5 @@ extern "C" int dfcsr_probe_fma(int fp64, int64_t iters, void *sink, double *flop
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }
+
+DFCSR_BOUNDS_READER(probe)

@@ -68,6 +68,11 @@ __device__ __forceinline__ void lattice_lerp(const dfcsr_wake_job &J, double s, 
         for (int k = 0; k < 6; ++k) out[k] = 0.0;
         return;
     }
+    if (!(bounds_ok(a, J.nsample, BS_ORBIT) && bounds_ok(b, J.nsample, BS_ORBIT))) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) out[k] = 0.0;
+        return;
+    }
     const double *pa = J.lattice + (size_t)a * 6, *pb = J.lattice + (size_t)b * 6;
 #pragma unroll
     for (int k = 0; k < 6; ++k) out[k] = pa[k] * (1 - f) + pb[k] * f;
@@ -103,6 +108,15 @@ __device__ __forceinline__ int ring_slot(const dfcsr_wake_job &J, int t) {
     return s;
 }
 
+// Checked build: the ring coordinates of a trilinear gather inside the ring
+// (slots < cap, x < nx, z < nz).
+__device__ __forceinline__ bool ring_cells_ok(const dfcsr_wake_job &J, int s0, int s1, int x0, int x1,
+                                              int z0, int z1) {
+    return bounds_ok(s0, J.cap, BS_FP64_RING) && bounds_ok(s1, J.cap, BS_FP64_RING) &&
+           bounds_ok(x0, J.nx, BS_FP64_RING) && bounds_ok(x1, J.nx, BS_FP64_RING) &&
+           bounds_ok(z0, J.nz, BS_FP64_RING) && bounds_ok(z1, J.nz, BS_FP64_RING);
+}
+
 // interpolate3D of one field of the history at (t, x, z), FP64 arithmetic,
 // reading the FP64 ring when present, else the FP32 ring.
 __device__ inline double hist_field_fp64(const dfcsr_wake_job &J, int field, double t, double x, double z) {
@@ -113,6 +127,7 @@ __device__ inline double hist_field_fp64(const dfcsr_wake_job &J, int field, dou
         !axis_index((z - J.z_min) / J.z_delta, J.nz, z0, z1, zd))
         return 0.0;
     const int s0 = ring_slot(J, t0), s1 = ring_slot(J, t1);
+    if (!ring_cells_ok(J, s0, s1, x0, x1, z0, z1)) return 0.0;
     auto D = [&](int s, int xi, int zi) -> double {
         const size_t cell = ((size_t)s * J.nx + xi) * J.nz + zi;
         return J.ring64 ? J.ring64[cell * 5 + field] : ring32_value(J.ring32, cell, field);
@@ -140,6 +155,7 @@ __device__ __forceinline__ void gather5_fp64(const dfcsr_wake_job &J, double t, 
         !axis_index((z - J.z_min) / J.z_delta, J.nz, z0, z1, zd))
         return;
     const int s0 = ring_slot(J, t0), s1 = ring_slot(J, t1);
+    if (!ring_cells_ok(J, s0, s1, x0, x1, z0, z1)) return;
     const size_t nz = J.nz, nxz = (size_t)J.nx * J.nz;
     const size_t c[8] = {(size_t)s0 * nxz + (size_t)x0 * nz + z0, (size_t)s1 * nxz + (size_t)x0 * nz + z0,
                          (size_t)s0 * nxz + (size_t)x0 * nz + z1, (size_t)s1 * nxz + (size_t)x0 * nz + z1,

@@ -182,3 +182,5 @@ extern "C" int dfcsr_wake_fp64(const dfcsr_wake_job *jobs, const int32_t *job_of
     DFCSR_LAUNCH_CHECK();
     return DFCSR_OK;
 }
+
+DFCSR_BOUNDS_READER(wake_fp64)

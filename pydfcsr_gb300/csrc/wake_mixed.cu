@@ -144,6 +144,9 @@ __device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *
 
 // One history field at (slot, x, z) from the FP64 ring, else the FP32 ring.
 __device__ __forceinline__ double hist_cell(const dfcsr_wake_job &J, int field, int slot, int xi, int zi) {
+    if (!(bounds_ok(slot, J.cap, BS_MIXED_SETUP) && bounds_ok(xi, J.nx, BS_MIXED_SETUP) &&
+          bounds_ok(zi, J.nz, BS_MIXED_SETUP)))
+        return 0.0;
     const size_t cell = ((size_t)slot * J.nx + xi) * J.nz + zi;
     return J.ring64 ? J.ring64[cell * 5 + field] : ring32_value(J.ring32, cell, field);
 }
@@ -205,6 +208,7 @@ __device__ __noinline__ void column_dw(const dfcsr_wake_job &J, const GeoShared 
         if (a0 < 0) a0 = 0;
         if (a0 > J.nsample - 1) a0 = J.nsample - 1;
         const dw f = dw_add_f(u, -(float)a0);
+        if (!bounds_ok(a0, J.nsample, BS_ORBIT)) a0 = 0;
         const float2 *P = reinterpret_cast<const float2 *>(J.lattice_dw) + (size_t)a0 * 6;
         const float2 *D = reinterpret_cast<const float2 *>(J.lattice_delta_dw) + (size_t)a0 * 6;
 #pragma unroll
@@ -484,7 +488,7 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
                 wgt = td;
             }
         } else if (l < 10) {
-            if (lat_in) {
+            if (lat_in && bounds_ok(a0, J.nsample, BS_ORBIT) && bounds_ok(a1, J.nsample, BS_ORBIT)) {
                 pa = J.lattice[(size_t)a0 * 6 + (l - 4)];
                 pb = J.lattice[(size_t)a1 * 6 + (l - 4)];
                 wgt = lf;
@@ -707,6 +711,12 @@ mixed_geometry(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
     float *prec = rec + (size_t)b * rec_words;
     const int ncols = gs.col_begin[nreg];
     const int nrows = gs.row_begin[nreg];
+    for (int r = 0; r < nreg; ++r)   // checked build: every record inside the point's words
+        if (!(bounds_ok((long long)gs.rm[r].col_off + (long long)gs.rm[r].nsp * CW - 1,
+                        (long long)rec_words, BS_GEO_REC) &&
+              bounds_ok((long long)gs.rm[r].row_off + (long long)gs.rm[r].nxp * RW - 1,
+                        (long long)rec_words, BS_GEO_REC)))
+            return;
     if (use_dw) {
         // observer velocity direction v = tau(s) + vx n(s), FP32 double-word
         const dw vxo = dw_add(gs.tsx, dw_mul(gs.vxw, gs.nsx));
@@ -1023,6 +1033,11 @@ __device__ __forceinline__ void chunk_points(const IntegralSmem &sm, const float
             int s0 = V.head + t0, s1 = V.head + t1;
             if (s0 >= V.cap) s0 -= V.cap;
             if (s1 >= V.cap) s1 -= V.cap;
+            if (!(bounds_ok(s0, V.cap, BS_MIXED_RING) && bounds_ok(s1, V.cap, BS_MIXED_RING) &&
+                  bounds_ok(x0, V.nx, BS_MIXED_RING) &&
+                  bounds_ok(x0 + __float_as_int(rw.y), V.nx, BS_MIXED_RING) &&
+                  bounds_ok(z0, V.nz, BS_MIXED_RING) && bounds_ok(z1, V.nz, BS_MIXED_RING)))
+                continue;
             const uint32_t c0x0 = ((uint32_t)s0 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
             const uint32_t c1x0 = ((uint32_t)s1 * (uint32_t)V.nx + (uint32_t)x0) * nzc + 2u * (uint32_t)z0;
             const uint32_t dxc = (uint32_t)__float_as_int(rw.y) * nzc;
@@ -1131,7 +1146,12 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
             V.inv_dt = dw{m->inv_dt_hi, m->inv_dt_lo};
             V.inv_dz = dw{m->inv_dz_hi, m->inv_dz_lo};
             const RegionMeta R = m->reg[r];
-            const int2 rv = rows_valid[b * WAKE_MAX_REGIONS + r];
+            int2 rv = rows_valid[b * WAKE_MAX_REGIONS + r];
+            if (rv.y > rv.x &&
+                !(bounds_ok(rv.x, R.nxp, BS_MIXED_ROWS) && bounds_ok(rv.y - 1, R.nxp, BS_MIXED_ROWS) &&
+                  bounds_ok((long long)R.row_off + (long long)R.nxp * RW - 1, (long long)rec_words, BS_MIXED_REC) &&
+                  bounds_ok((long long)R.col_off + (long long)R.nsp * CW - 1, (long long)rec_words, BS_MIXED_REC)))
+                rv.y = rv.x;   // checked build: skip the region
             dw reg_z{0.f, 0.f}, reg_x{0.f, 0.f};
             if (rv.y > rv.x) {
                 const float4 *rb = reinterpret_cast<const float4 *>(base + R.row_off);
@@ -1452,3 +1472,5 @@ extern "C" int dfcsr_wake_mixed_job(const dfcsr_wake_job *job, const double *s, 
     return wake_mixed_run(nullptr, job, nullptr, s, x, n, xbins_max, zbins_max, use_band, dE, xkick,
                           workspace, workspace_bytes, stream);
 }
+
+DFCSR_BOUNDS_READER(wake_mixed)

@@ -35,6 +35,24 @@ def test_every_header_symbol_exported():
     assert set(names) <= set(_lib.EXPORTS), set(names) - set(_lib.EXPORTS)
 
 
+def test_bounds_checked_library_builds_and_exports():
+    """The bounds-checked variant builds from the same sources and exports
+    the same symbols; it reports itself as checked, the release library not.
+    In the release library the status query answers without a device."""
+    path = build.build(checked=True)
+    assert path != build.build() and os.path.exists(path)
+    chk = ctypes.CDLL(path)
+    for n in header_functions():
+        assert hasattr(chk, n), f"{n} missing from the checked library"
+    assert chk.dfcsr_bounds_checked() == 1
+    lib = _lib.load()
+    assert lib.dfcsr_bounds_checked() == 0
+    assert _lib.bounds_status(reset=True) is None
+    assert "bounds_status" in dir(_lib)
+    with pytest.raises(_lib.DfcsrBadArgument, match="site"):
+        _lib.call("dfcsr_bounds_probe", 0, 1, 0, None)
+
+
 def test_launch_counter_without_gpu():
     """The launch counter is host-side: readable without a device, and an
     argument error launches nothing."""
