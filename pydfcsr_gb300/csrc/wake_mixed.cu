@@ -1120,6 +1120,9 @@ mixed_integral(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restric
     // work unit = one integration region of one point (unit u: point
     // u / WAKE_MAX_REGIONS, region u % WAKE_MAX_REGIONS), so that the CTAs
     // finish a batch together (a region is a quarter to a half of a point).
+    // Region-major order instead (all far regions first, so that the last
+    // units of a launch are the small ones) measured 2 % slower per 4-region
+    // step (1.747 vs 1.715 ms).
     // The next unit's index is taken while the current one runs, so the
     // atomic's latency is off the CTA's critical path: slot par holds the
     // current unit, slot par ^ 1 receives the next before the unit-end
