@@ -358,8 +358,10 @@ int dfcsr_wake_integrand(const dfcsr_wake_job *job, double s, double x,
  * double-word, the rest Kahan-compensated FP32; fixed-order block sums,
  * region sums in FP64.  Max, rms and pointwise error vs the FP64 kernel on
  * the same history <= 2e-5 of the peak on the benchmark workloads.  Needs
- * ring32 in every job (below 64 GiB: cells are addressed with 32-bit
- * offsets).  xbins_max / zbins_max
+ * ring32 in every job, below 64 GiB (cap * nx * nz * 2 <= 2^32 - 1: cells
+ * are addressed with 32-bit float4 offsets; a larger ring makes the job's
+ * points NaN, and dfcsr_wake_mixed_job refuses it with DFCSR_BAD_ARG).
+ * xbins_max / zbins_max
  * bound the integration bins of all jobs in the call.  use_band != 0 runs
  * the s' columns with |s' - s| < job.near_band through the FP64 integrand.
  * Scratch: dfcsr_wake_workspace_bytes(xbins_max, zbins_max, n); points are

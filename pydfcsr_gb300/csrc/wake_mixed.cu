@@ -142,6 +142,12 @@ __device__ __forceinline__ void layout(const Region *reg, int nreg, RegionMeta *
     if ((size_t)off > rec_words) ok = false;
 }
 
+// The integral's history-cell offsets are 32-bit counts of float4 (two per
+// 32-byte cell): the FP32 ring must hold fewer than 2^32 of them (64 GiB).
+__host__ __device__ __forceinline__ bool ring32_offsets_fit(long long cap, long long nx, long long nz) {
+    return cap >= 0 && nx >= 0 && nz >= 0 && cap * nx * nz * 2 <= 0xFFFFFFFFll;
+}
+
 // One history field at (slot, x, z) from the FP64 ring, else the FP32 ring.
 __device__ __forceinline__ double hist_cell(const dfcsr_wake_job &J, int field, int slot, int xi, int zi) {
     if (!(bounds_ok(slot, J.cap, BS_MIXED_SETUP) && bounds_ok(xi, J.nx, BS_MIXED_SETUP) &&
@@ -555,6 +561,9 @@ mixed_setup(const dfcsr_wake_job *__restrict__ jobs, const int32_t *__restrict__
             // the integral reads 32-byte cells with one 256-bit load: a ring
             // that is not 32-byte aligned makes the point invalid (NaN result)
             if (((uintptr_t)J.ring32 & 31u) != 0) ok = false;
+            // and forms cell offsets in 32-bit float4 units: a ring of more
+            // than 2^32 of them (64 GiB) makes the point invalid too
+            if (!ring32_offsets_fit(J.cap, J.nx, J.nz)) ok = false;
             gs.ok = ok ? 1 : 0;
             int cb = 0, rb = 0;
             for (int r = 0; r < gs.nreg; ++r) {
@@ -1472,6 +1481,9 @@ extern "C" int dfcsr_wake_mixed_job(const dfcsr_wake_job *job, const double *s, 
                                     void *stream) {
     clear_error();
     DFCSR_CHECK_ARG(n == 0 || job, "dfcsr_wake_mixed_job: null job");
+    DFCSR_CHECK_ARG(n == 0 || ring32_offsets_fit(job->cap, job->nx, job->nz),
+                    "dfcsr_wake_mixed_job: the FP32 history ring (%d slots of %d x %d cells) exceeds "
+                    "the 64 GiB its 32-bit cell offsets address", job->cap, job->nx, job->nz);
     return wake_mixed_run(nullptr, job, nullptr, s, x, n, xbins_max, zbins_max, use_band, dE, xkick,
                           workspace, workspace_bytes, stream);
 }

@@ -116,6 +116,12 @@ def test_bad_arguments_fail_without_gpu():
         _lib.call("dfcsr_wake_mixed_job", ctypes.byref(job), ctypes.c_void_p(16),
                   ctypes.c_void_p(16), 5, 2000, 100, 0, ctypes.c_void_p(16), ctypes.c_void_p(16),
                   None, 0, None)
+    big = _lib.WakeJob()
+    big.cap, big.nx, big.nz = 5000, 1000, 1000        # 1e10 float4 of FP32 ring
+    with pytest.raises(_lib.DfcsrBadArgument, match="64 GiB"):
+        _lib.call("dfcsr_wake_mixed_job", ctypes.byref(big), ctypes.c_void_p(16),
+                  ctypes.c_void_p(16), 5, 100, 100, 0, ctypes.c_void_p(16), ctypes.c_void_p(16),
+                  None, 0, None)
     with pytest.raises(_lib.DfcsrBadArgument, match="null job"):
         _lib.call("dfcsr_wake_mixed_job", None, ctypes.c_void_p(16), ctypes.c_void_p(16), 5, 100,
                   100, 0, ctypes.c_void_p(16), ctypes.c_void_p(16), None, 0, None)
