@@ -60,8 +60,9 @@ size_t dfcsr_abi_sizeof(int which);
  * gathers, 31 orbit tables, 40-43
  * deposit, 50 history regrid, 60 apply_wakes, 70 DF stage, 80 interp3d /
  * interp1d.  dfcsr_bounds_checked: 1 in the checked library, 0 otherwise.
- * dfcsr_bounds_status: synchronises the device and gives the first failure
- * (0: none), clearing the status words when `reset`; in the release library
+ * dfcsr_bounds_status: synchronises the current device and gives the first
+ * failure recorded on it (0: none; the status words are per device),
+ * clearing them when `reset`; in the release library
  * it gives 0 without touching the device.  dfcsr_bounds_probe: one thread
  * tests `index` against [0, size) at `site` (1..32767) through the same
  * check, without accessing memory (a test of the mechanism itself). */
