@@ -1,6 +1,7 @@
 """The benchmark's roofline arithmetic (host only): integrand points counted
 per timed step from the branch each step took, the FP32 operation rate
-against the measured peak, and the instruction-issue ceiling."""
+against the measured peak, and the instruction-issue ceiling; and the
+reference arm's JSON line, run on the CPU."""
 from types import SimpleNamespace
 
 import pytest
@@ -39,3 +40,27 @@ def test_roofline_mixed_fields():
 
 def test_issue_bound_needs_a_clock():
     assert bench.issue_bound(1e6, 1.0, None, 152) is None
+
+
+def test_reference_arm_line_on_cpu():
+    """`bench.py --impl reference` (the reference's CPU algorithm, the
+    oracle here, on the host cores) prints one JSON line with the GPU arm's
+    metric, unit and direction, impl "reference", its cpu_baseline and an
+    e2e object without host<->device bytes.  A small beam keeps it short."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "1", "--particles", "20000"],
+                       capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+    assert line["impl"] == "reference"
+    assert line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["higher_is_better"] is True and line["value"] > 0
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["cores"] >= 1 and cb["kind"] in ("port", "reference")
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["unit"] == line["unit"]
